@@ -1,0 +1,154 @@
+/*
+ * volumefluxes_sm103.h -- C ABI of the GB300 (sm_103a) shallow-water step library.
+ *
+ * One handle owns one 2D simulation on one CUDA device: its state buffers,
+ * bottom topography, time-derivative scratch and a device-resident step
+ * record (time, dt, CFL maxima). The entry points below are what a
+ * VolumeFluxes.jl backend binds with `ccall` to replace the reference's
+ * per-loop KernelAbstractions launches; each cites the reference interface it
+ * stands in for (paths are within the VolumeFluxes.jl project).
+ *
+ * Conventions
+ *  - All functions return 0 on success and a negative VF_E* code on failure;
+ *    vf_last_error() gives a message. Nothing aborts, nothing traps on the
+ *    device.
+ *  - Host arrays use the reference's Volume layout: one plane per variable
+ *    (w, hu, hv), each column-major with x fastest
+ *    (src/volume/volume.jl:24-51, src/backends/buffer.jl:29-42). Element type
+ *    is double for real_bytes == 8 and float for real_bytes == 4.
+ *  - Host pointers need only be valid for the duration of the call. Calls on
+ *    one handle are synchronous and not reentrant; distinct handles may be
+ *    used from distinct threads.
+ */
+#ifndef VOLUMEFLUXES_SM103_H
+#define VOLUMEFLUXES_SM103_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VF_ABI_VERSION 1
+#define VF_MAX_SOURCES 8
+
+/* Error codes. */
+#define VF_OK 0
+#define VF_EINVAL (-1)   /* invalid argument or unsupported configuration */
+#define VF_ENOMEM (-2)   /* device or host allocation failed */
+#define VF_ECUDA (-3)    /* CUDA runtime error */
+#define VF_ESTATE (-4)   /* call out of order (e.g. stepping before a state upload) */
+
+/* Source terms, applied in the order listed
+ * (src/system.jl:62-75: directional terms inside the x/y loop, the rest after). */
+#define VF_SRC_BOTTOM 1       /* SourceTermBottom, src/sourceterms/source_term_bottom.jl:24-41 */
+#define VF_SRC_CONST_RAIN 2   /* ConstantRain(rate [m/h]), src/sourceterms/source_term_rain.jl:24-30,71-76 */
+#define VF_SRC_CONST_INFIL 3  /* ConstantInfiltration(rate [m/s]), src/sourceterms/source_term_infiltration.jl:73-88 */
+
+/* ImplicitFriction laws, src/friction.jl:30-43. */
+#define VF_FRICTION_NONE 0
+#define VF_FRICTION_BSA2012 1
+#define VF_FRICTION_FCG2016 2
+#define VF_FRICTION_BH2021 3
+
+#define VF_STEPPER_FE 1       /* ForwardEulerStepper, src/timestepper/forwardeuler.jl:23-47 */
+#define VF_STEPPER_RK2 2      /* RungeKutta2, src/timestepper/rungekutta.jl:21-52 */
+#define VF_BC_WALL 1          /* WallBC, src/bc.jl:81-110 */
+#define VF_REC_LINEAR 1       /* LinearReconstruction(theta), src/reconstruction/linearreconstruction.jl:22-102 */
+
+/* Everything the reference's ConservedSystem + Simulator constructors carry
+ * for this path (src/system.jl:37-53, src/simulator.jl:72-91,
+ * src/equations/swe_2D.jl:28, src/grid.jl:82-90). */
+typedef struct vf_config {
+  int32_t abi_version;       /* VF_ABI_VERSION */
+  int32_t nx, ny, gc;        /* interior cells and ghost layers (gc must be 2) */
+  double extent[4];          /* x0, x1, y0, y1 */
+  int32_t real_bytes;        /* 8: Float64 state, 4: Float32 state */
+  double g, rho, depth_cutoff, desingularizing_kappa;
+  int32_t reconstruction;    /* VF_REC_LINEAR */
+  double theta;
+  int32_t n_sources;
+  int32_t source_kind[VF_MAX_SOURCES];
+  double source_rate[VF_MAX_SOURCES];
+  int32_t friction;          /* VF_FRICTION_* */
+  double friction_Cz;
+  int32_t stepper;           /* VF_STEPPER_* */
+  int32_t bc;                /* VF_BC_WALL */
+  double cfl;
+  int32_t bottom_is_constant;/* 1: ConstantBottomTopography(bottom_constant) */
+  double bottom_constant;
+  int32_t device;            /* CUDA device ordinal */
+} vf_config;
+
+typedef struct vf_handle vf_handle;
+
+/* Stands in for ConservedSystem(...) + Simulator(backend, system, stepper, grid; cfl)
+ * (src/system.jl:37-53, src/simulator.jl:72-91) with create_buffer on the
+ * device (src/backends/buffer.jl:40-42). Validates the configuration the way
+ * the reference's constructors do (gc > 1 for LinearReconstruction,
+ * src/reconstruction/linearreconstruction.jl:59; is_compatible,
+ * src/equations/equation.jl:74-84). */
+int vf_create(const vf_config* cfg, vf_handle** out);
+void vf_destroy(vf_handle* h);
+
+/* Stands in for BottomTopography2D(B, backend, grid): convert_to_backend of the
+ * corner array (src/bottom_topography.jl:51-57), (nx+2gc+1) x (ny+2gc+1),
+ * x fastest. */
+int vf_upload_bottom(vf_handle* h, const void* B_corners);
+
+/* Stands in for set_current_state!(sim, state) (src/simulator.jl:119-135):
+ * writes the interior planes (nx*ny each, x fastest), then the device
+ * boundary update (src/bc.jl:81-110). */
+int vf_set_interior_state(vf_handle* h, const void* w, const void* hu, const void* hv);
+/* Full-volume upload (ghost cells included), 3 planes of (nx+2gc)*(ny+2gc). */
+int vf_upload_state(vf_handle* h, const void* state);
+/* Stands in for collect(current_state(sim)) (src/simulator.jl:98). */
+int vf_download_state(vf_handle* h, void* state);
+/* Stands in for collect(current_interior_state(sim).h/.hu/.hv)
+ * (src/simulator.jl:114-115, src/volume/interior_volume_variable.jl:168-176).
+ * Any of the three pointers may be NULL. */
+int vf_get_interior_state(vf_handle* h, void* w, void* hu, void* hv);
+
+/* Stands in for perform_step!(sim, max_dt) (src/simulator.jl:145-177): one
+ * full FE/RK2 step including friction, dry clamp and boundary update. Writes
+ * the dt used (current_timestep) to *dt_out. Does not advance the handle's
+ * time; the caller does t += dt as simulate_to_time does (src/simulator.jl:205). */
+int vf_step(vf_handle* h, double max_dt, double* dt_out);
+
+/* Stands in for the loop of simulate_to_time (src/simulator.jl:179-212) with
+ * the time kept on the device: from t0, step while t < endtime with
+ * max_dt = endtime - t when match_endtime (else +Inf), capped by
+ * maximum_timestep when it is >= 0. Stops early, after the step where
+ * t + dt >= stop_time (the IntervalWriter trigger, src/callbacks.jl:49-55),
+ * or after max_steps steps when max_steps > 0. No host synchronisation
+ * happens between steps. Outputs (any may be NULL): final time, steps taken,
+ * dt of the last step. */
+int vf_simulate(vf_handle* h, double t0, double endtime, int32_t match_endtime, double maximum_timestep,
+                double stop_time, int64_t max_steps, double* t_out, int64_t* steps_out, double* last_dt_out);
+
+/* Total water volume sum((w - B_cell) * dx * dy) over the interior, summed in
+ * Float64 on the device in a fixed order (the water-volume bookkeeping of
+ * examples/example_tools.jl:49-106). */
+int vf_water_volume(vf_handle* h, double* out);
+
+/* Device-resident access for callers that keep data on the GPU: the current
+ * state's device base pointer, its row pitch and plane stride in elements,
+ * and the element offset of total cell (0, 0). Valid until the next step. */
+int vf_device_state(vf_handle* h, void** base, int64_t* pitch, int64_t* plane_stride, int64_t* offset00);
+/* The CUDA stream all of the handle's work is issued on (cudaStream_t). */
+int vf_stream(vf_handle* h, void** stream);
+
+/* Times n_steps steps already resident on the device with CUDA events on the
+ * handle's stream (no host copies); writes the elapsed milliseconds. Uses
+ * match_endtime = false and max_dt = +Inf, as perform_step!(sim, Inf). */
+int vf_time_steps(vf_handle* h, int64_t n_steps, float* ms_out);
+
+/* Message for the last failure on this handle (or of vf_create when h is NULL). */
+const char* vf_last_error(vf_handle* h);
+/* Kernel launches issued by this handle since creation. */
+int64_t vf_launch_count(vf_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

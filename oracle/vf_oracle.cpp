@@ -1,0 +1,686 @@
+/*
+ * vf_oracle.cpp -- CPU oracle for VolumeFluxes.jl's practical 2D shallow-water step.
+ *
+ * TEST INFRASTRUCTURE ONLY: a restatement of the reference's CPU path used to
+ * check the CUDA library and as the timed CPU baseline. The product library
+ * never links or calls this file.
+ *
+ * Every pass mirrors one reference loop, in the reference's order, with the
+ * reference's per-element expression order (no FMA contraction: build with
+ * -ffp-contract=off). Passes that the reference runs over all cells
+ * (zeroing, rain, infiltration, Euler update, RK2 average, friction, dry
+ * clamp) run over all cells here too. Each face flux is evaluated twice, as in
+ * src/numericalflux/numericalflux.jl:24-30. Citations are path:line within
+ * the reference project; line numbers include the 20-line licence header.
+ *
+ * Parity pin: the reference publishes no golden fields. The oracle is pinned
+ * by the reference's own known-answer tests for this path (minmod,
+ * bottom-topography lookups, wall-BC mapping, lake at rest, rain
+ * accumulation, infiltration drawdown, mirror symmetry), ported under tests/.
+ *
+ * cbrt (Manning-type friction laws) is evaluated correctly rounded; Julia's
+ * cbrt is accurate to < 1 ulp, so the two agree except where Julia's result
+ * is not the nearest double.
+ */
+#include "vf_oracle.h"
+
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Julia's IEEE min/max: NaN-propagating, and -0.0 < +0.0.
+template <typename T>
+inline T jl_max(T x, T y) {
+  if (x != x || y != y) return x - y;
+  return (x > y || (x == y && !std::signbit(x))) ? x : y;
+}
+template <typename T>
+inline T jl_min(T x, T y) {
+  if (x != x || y != y) return x - y;
+  return (x < y || (x == y && std::signbit(x))) ? x : y;
+}
+
+// ---------------------------------------------------------------------------
+// Correctly rounded cube root of a double. A libm seed is corrected by an
+// exact integer test on the rounding midpoints, so the result is the unique
+// nearest double whatever the seed's last-bit error.
+struct U192 { uint64_t w[3]; };  // w[0] least significant
+
+inline int cmp192(const U192& a, const U192& b) {
+  for (int i = 2; i >= 0; --i) {
+    if (a.w[i] != b.w[i]) return a.w[i] < b.w[i] ? -1 : 1;
+  }
+  return 0;
+}
+
+inline U192 cube_u54(uint64_t k) {  // k < 2^55
+  unsigned __int128 sq = (unsigned __int128)k * k;             // < 2^110
+  uint64_t lo = (uint64_t)sq, hi = (uint64_t)(sq >> 64);
+  unsigned __int128 p0 = (unsigned __int128)k * lo;             // < 2^119
+  unsigned __int128 p1 = (unsigned __int128)k * hi;             // < 2^101
+  U192 r;
+  r.w[0] = (uint64_t)p0;
+  unsigned __int128 mid = (p0 >> 64) + (unsigned __int128)(uint64_t)p1;
+  r.w[1] = (uint64_t)mid;
+  r.w[2] = (uint64_t)(mid >> 64) + (uint64_t)(p1 >> 64);
+  return r;
+}
+
+inline U192 shl192(uint64_t m, int s) {  // m << s, 64 <= s < 128
+  U192 r;
+  r.w[0] = 0;
+  int t = s - 64;
+  r.w[1] = t == 0 ? m : (m << t);
+  r.w[2] = t == 0 ? 0 : (m >> (64 - t));
+  return r;
+}
+
+double cr_cbrt(double x) {
+  if (x == 0.0 || !std::isfinite(x)) return x;
+  const bool neg = std::signbit(x);
+  double a = std::fabs(x);
+  int extra = 0;  // result is scaled by 2^-extra
+  uint64_t bits;
+  std::memcpy(&bits, &a, 8);
+  if ((bits >> 52) == 0) {  // subnormal: scale by 2^54 (exact), result by 2^-18
+    a = a * 18014398509481984.0;
+    std::memcpy(&bits, &a, 8);
+    extra = 18;
+  }
+  int e = (int)(bits >> 52) - 1023;
+  uint64_t M = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+  int q = e >= 0 ? e / 3 : -((-e + 2) / 3);
+  int r = e - 3 * q;                          // 0, 1, 2
+  double t = std::ldexp((double)M, r - 52);  // exact, in [1, 8)
+  double y0 = std::cbrt(t);
+  uint64_t Y;
+  if (y0 >= 2.0) {
+    Y = 1ull << 53;
+  } else if (y0 < 1.0) {
+    Y = 1ull << 52;
+  } else {
+    uint64_t yb;
+    std::memcpy(&yb, &y0, 8);
+    Y = (yb & ((1ull << 52) - 1)) | (1ull << 52);
+  }
+  // cbrt(t) lies in [(2Y-1)/2^53, (2Y+1)/2^53) iff (2Y-1)^3 <= t*2^159 < (2Y+1)^3;
+  // t*2^159 = M * 2^(r+107). Odd cubes never equal it, so there are no ties.
+  const U192 T = shl192(M, r + 107);
+  for (int it = 0; it < 8; ++it) {
+    if (cmp192(cube_u54(2 * Y + 1), T) < 0) { ++Y; continue; }
+    if (Y > (1ull << 52) && cmp192(cube_u54(2 * Y - 1), T) > 0) { --Y; continue; }
+    break;
+  }
+  double y = std::ldexp((double)Y, q - 52 - extra);
+  return neg ? -y : y;
+}
+
+inline float cr_cbrt(float x) { return (float)cr_cbrt((double)x); }
+
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Sim {
+  vfo_params p;
+  int N1, N2;          // total cells per direction
+  size_t plane;        // N1*N2
+  double dx, dy;       // grid spacing, Float64 as in src/grid.jl:82-90
+  std::vector<double> B;  // corners (N1+1)*(N2+1), Float64
+  // State buffers U[0..nsub]; left/right face buffers; wavespeed scalar field.
+  std::vector<std::vector<T>> U;
+  std::vector<T> left, right, ws;
+  double t;
+  double current_dt;
+  // Equation constants in the state's real type.
+  T g, rho, cutoff, kappa, theta, cfl;
+
+  size_t id(int i, int j) const { return (size_t)i + (size_t)N1 * (size_t)j; }
+};
+
+template <typename T>
+struct Ops {
+  Sim<T>& s;
+  explicit Ops(Sim<T>& sim) : s(sim) {}
+
+  // --- bottom topography lookups, src/bottom_topography.jl:86-101 ----------
+  // 0-based cell (i, j) uses 0-based corners (i..i+1, j..j+1).
+  T Bc(int i, int j) const {
+    if (s.p.bottom_is_constant) return (T)s.p.bottom_constant;
+    const int W = s.N1 + 1;
+    const double* B = s.B.data();
+    return (T)(0.25 * (B[i + W * j] + B[i + 1 + W * j] + B[i + W * (j + 1)] + B[i + 1 + W * (j + 1)]));
+  }
+  T Bl(int i, int j, int dir) const {
+    if (s.p.bottom_is_constant) return (T)s.p.bottom_constant;
+    const int W = s.N1 + 1;
+    const double* B = s.B.data();
+    if (dir == 0) return (T)(0.5 * (B[i + W * j] + B[i + W * (j + 1)]));
+    return (T)(0.5 * (B[i + W * j] + B[i + 1 + W * j]));
+  }
+  T Br(int i, int j, int dir) const {
+    if (s.p.bottom_is_constant) return (T)s.p.bottom_constant;
+    const int W = s.N1 + 1;
+    const double* B = s.B.data();
+    if (dir == 0) return (T)(0.5 * (B[i + 1 + W * j] + B[i + 1 + W * (j + 1)]));
+    return (T)(0.5 * (B[i + W * (j + 1)] + B[i + 1 + W * (j + 1)]));
+  }
+
+  // --- src/equations/equation.jl:40-67 -------------------------------------
+  T desing(T h) const {
+    const T k = s.kappa;
+    T m = jl_min<T>(h * h / ((T)2 * k) + k / (T)2.0, k);
+    return std::copysign((T)1, h) * jl_max<T>(std::fabs(h), m);
+  }
+
+  // --- src/equations/swe_2D.jl:43-65 ---------------------------------------
+  void phys_flux(int dir, const T* q, T* F) const {
+    const T h = q[0];
+    const T u = q[1] / desing(h);
+    const T v = q[2] / desing(h);
+    const T rho = s.rho, g = s.g;
+    const T hh = h * h;
+    if (dir == 0) {
+      F[0] = rho * h * u;
+      F[1] = rho * h * u * u + (T)0.5 * rho * g * hh;
+      F[2] = rho * h * u * v;
+    } else {
+      F[0] = rho * h * v;
+      F[1] = rho * h * u * v;
+      F[2] = rho * h * v * v + (T)0.5 * rho * g * hh;
+    }
+  }
+  // --- src/equations/swe_2D.jl:69-81 ---------------------------------------
+  void eigen(int dir, const T* q, T* e) const {
+    const T h = q[0];
+    const T u = (dir == 0 ? q[1] : q[2]) / desing(h);
+    e[0] = u + std::sqrt(s.g * h);
+    e[1] = u - std::sqrt(s.g * h);
+    e[2] = u;
+  }
+
+  // --- src/numericalflux/swe/centralupwind.jl:48-77 ------------------------
+  T central_upwind(const T* fminus, const T* fplus, int dir, T* F) const {
+    T flm[3] = {0, 0, 0}, em[3] = {0, 0, 0};
+    if (fminus[0] > s.cutoff) {
+      phys_flux(dir, fminus, flm);
+      eigen(dir, fminus, em);
+    }
+    T flp[3] = {0, 0, 0}, ep[3] = {0, 0, 0};
+    if (fplus[0] > s.cutoff) {
+      phys_flux(dir, fplus, flp);
+      eigen(dir, fplus, ep);
+    }
+    const T aplus = jl_max<T>(jl_max<T>(ep[0], em[0]), (T)0);
+    const T aminus = jl_min<T>(jl_min<T>(ep[1], em[1]), (T)0);
+    if (std::fabs(aplus - aminus) < s.kappa) {
+      F[0] = F[1] = F[2] = 0;
+      return 0;
+    }
+    for (int k = 0; k < 3; ++k) {
+      F[k] = (aplus * flm[k] - aminus * flp[k]) / (aplus - aminus) +
+             ((aplus * aminus) / (aplus - aminus)) * (fplus[k] - fminus[k]);
+    }
+    if (fminus[0] < s.cutoff && fplus[0] < s.cutoff) return 0;
+    return jl_max<T>(std::fabs(aplus), std::fabs(aminus));
+  }
+
+  // --- src/reconstruction/linearreconstruction.jl:28-43 --------------------
+  static T minmod(T a, T b, T c) {
+    if (a > 0 && b > 0 && c > 0) return jl_min<T>(jl_min<T>(a, b), c);
+    if (a < 0 && b < 0 && c < 0) return jl_max<T>(jl_max<T>(a, b), c);
+    return 0;
+  }
+  static T minmod_slope(T l, T c, T r, T theta) {
+    const T fwd = r - c;
+    const T bwd = c - l;
+    const T central = (fwd + bwd) / (T)2.0;
+    return minmod(theta * fwd, central, theta * bwd);
+  }
+
+  // Buffer access: plane k of a 3-plane array.
+  T& at(std::vector<T>& a, int k, int i, int j) const { return a[(size_t)k * s.plane + s.id(i, j)]; }
+  T at(const std::vector<T>& a, int k, int i, int j) const { return a[(size_t)k * s.plane + s.id(i, j)]; }
+
+  // --- src/reconstruction/linearreconstruction.jl:58-102 -------------------
+  // for_each_inner_cell(...; ghostcells=1): along dir, cells 1..N-2 (0-based);
+  // across, the interior (src/grid.jl:213-244).
+  void reconstruct(const std::vector<T>& Uin, int dir) {
+    const int gc = s.p.gc;
+    const int ilo = dir == 0 ? 1 : gc, ihi = dir == 0 ? s.N1 - 1 : gc + s.p.nx;
+    const int jlo = dir == 0 ? gc : 1, jhi = dir == 0 ? gc + s.p.ny : s.N2 - 1;
+    const int di = dir == 0 ? 1 : 0, dj = dir == 0 ? 0 : 1;
+#pragma omp parallel for schedule(static)
+    for (int j = jlo; j < jhi; ++j) {
+      for (int i = ilo; i < ihi; ++i) {
+        T slope[3];
+        for (int k = 0; k < 3; ++k)
+          slope[k] = minmod_slope(at(Uin, k, i - di, j - dj), at(Uin, k, i, j), at(Uin, k, i + di, j + dj), s.theta);
+        const T B_left = Bl(i, j, dir);
+        const T B_right = Br(i, j, dir);
+        const T w = at(Uin, 0, i, j);
+        if (w - (T)0.5 * slope[0] < B_left) {
+          slope[0] = (T)2.0 * (w - B_left);
+        } else if (w + (T)0.5 * slope[0] < B_right) {
+          slope[0] = (T)2.0 * (B_right - w);
+        }
+        for (int k = 0; k < 3; ++k) {
+          at(s.left, k, i, j) = at(Uin, k, i, j) - (T)0.5 * slope[k];
+          at(s.right, k, i, j) = at(Uin, k, i, j) + (T)0.5 * slope[k];
+        }
+        at(s.left, 0, i, j) = at(s.left, 0, i, j) - B_left;
+        at(s.right, 0, i, j) = at(s.right, 0, i, j) - B_right;
+      }
+    }
+  }
+
+  // --- src/numericalflux/numericalflux.jl:21-33 ----------------------------
+  T compute_flux(std::vector<T>& out, int dir) {
+    const int gc = s.p.gc;
+    const double delta = dir == 0 ? s.dx : s.dy;
+    const T inv = (T)(1 / delta);
+    const int di = dir == 0 ? 1 : 0, dj = dir == 0 ? 0 : 1;
+#pragma omp parallel for schedule(static)
+    for (int j = gc; j < gc + s.p.ny; ++j) {
+      for (int i = gc; i < gc + s.p.nx; ++i) {
+        T rm[3], lr[3], rl[3], lm[3];
+        for (int k = 0; k < 3; ++k) {
+          rm[k] = at(s.right, k, i, j);
+          lr[k] = at(s.left, k, i + di, j + dj);
+          rl[k] = at(s.right, k, i - di, j - dj);
+          lm[k] = at(s.left, k, i, j);
+        }
+        T Fr[3], Fl[3];
+        const T sr = central_upwind(rm, lr, dir, Fr);
+        const T sl = central_upwind(rl, lm, dir, Fl);
+        for (int k = 0; k < 3; ++k) at(out, k, i, j) = at(out, k, i, j) - inv * (Fr[k] - Fl[k]);
+        s.ws[s.id(i, j)] = jl_max<T>(sr, sl);
+      }
+    }
+    // maximum(wavespeeds) over the whole buffer; ghost entries stay 0.
+    T m = s.ws[0];
+    for (size_t n = 1; n < s.plane; ++n) m = jl_max<T>(m, s.ws[n]);
+    return m;
+  }
+
+  // --- src/sourceterms/source_term_bottom.jl:24-41 -------------------------
+  void bottom_source(std::vector<T>& out, int dir) {
+    const int gc = s.p.gc;
+    const T delta = (T)(dir == 0 ? s.dx : s.dy);
+    const int k = dir == 0 ? 1 : 2;
+#pragma omp parallel for schedule(static)
+    for (int j = gc; j < gc + s.p.ny; ++j) {
+      for (int i = gc; i < gc + s.p.nx; ++i) {
+        const T B_right = Br(i, j, dir);
+        const T B_left = Bl(i, j, dir);
+        const T hr = at(s.right, 0, i, j), hl = at(s.left, 0, i, j);
+        at(out, k, i, j) = at(out, k, i, j) + -s.g * ((B_right - B_left) / delta) * ((hr + hl) / (T)2.0);
+      }
+    }
+  }
+
+  // --- src/sourceterms/source_term_rain.jl:71-76 / infiltration.jl:83-88 ---
+  void add_all_cells_h(std::vector<T>& out, T value, bool subtract) {
+    const size_t n = s.plane;
+#pragma omp parallel for schedule(static)
+    for (long long c = 0; c < (long long)n; ++c) {
+      out[c] = subtract ? out[c] - value : out[c] + value;
+    }
+  }
+
+  // --- src/system.jl:62-75 -------------------------------------------------
+  void add_time_derivative(std::vector<T>& out, const std::vector<T>& Uin, T* maxspeed) {
+    for (int dir = 0; dir < 2; ++dir) {
+      reconstruct(Uin, dir);
+      maxspeed[dir] = compute_flux(out, dir);
+      for (int n = 0; n < s.p.n_sources; ++n)
+        if (s.p.source_kind[n] == VFO_SRC_BOTTOM) bottom_source(out, dir);
+    }
+    for (int n = 0; n < s.p.n_sources; ++n) {
+      if (s.p.source_kind[n] == VFO_SRC_CONST_RAIN)
+        add_all_cells_h(out, (T)(s.p.source_rate[n] / 3600), false);
+      else if (s.p.source_kind[n] == VFO_SRC_CONST_INFIL)
+        add_all_cells_h(out, (T)s.p.source_rate[n], true);
+    }
+  }
+
+  // --- src/friction.jl:30-43, 62-84 ----------------------------------------
+  T friction_law(T c, T h, T speed) const {
+    switch (s.p.friction) {
+      case VFO_FRICTION_BSA2012: {
+        T denom = cr_cbrt(h) * h;
+        return -c * speed / denom;
+      }
+      case VFO_FRICTION_FCG2016: {
+        T denom = cr_cbrt(h) * h * h;
+        return -c * speed / denom;
+      }
+      default: {
+        T denom = h * h;
+        return -c * speed / denom;
+      }
+    }
+  }
+  void implicit_friction(std::vector<T>& out, const std::vector<T>& prev, double dt) {
+    const T Cz = (T)s.p.friction_Cz;
+    const T tdt = (T)dt;
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < s.N2; ++j) {
+      for (int i = 0; i < s.N1; ++i) {
+        const T h_star = desing(at(prev, 0, i, j) - Bc(i, j));
+        const T u = at(prev, 1, i, j) / h_star;
+        const T v = at(prev, 2, i, j) / h_star;
+        T speed = std::sqrt(u * u + v * v);
+        if (speed == 0) speed = 0;
+        const T S = friction_law(Cz, h_star, speed);
+        const T ff[3] = {(T)0, S, S};
+        for (int k = 0; k < 3; ++k) at(out, k, i, j) = at(out, k, i, j) / ((T)1 - tdt * ff[k]);
+      }
+    }
+  }
+
+  // --- src/timestepper/timestepper.jl:41-51 --------------------------------
+  void post_proc(std::vector<T>& out) {
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < s.N2; ++j) {
+      for (int i = 0; i < s.N1; ++i) {
+        const T b = Bc(i, j);
+        if (at(out, 0, i, j) - b < s.cutoff) {
+          at(out, 0, i, j) = jl_max<T>(at(out, 0, i, j), b);
+          at(out, 1, i, j) = 0;
+          at(out, 2, i, j) = 0;
+        }
+      }
+    }
+  }
+
+  // --- src/bc.jl:81-110 ----------------------------------------------------
+  void update_bc(std::vector<T>& d) {
+    const int gc = s.p.gc, N1 = s.N1, N2 = s.N2;
+    // X: ghost columns at interior rows.
+    for (int j = gc; j < gc + s.p.ny; ++j) {
+      for (int g = 1; g <= gc; ++g) {
+        const int lg = g - 1, li = 2 * gc + 1 - g - 1;
+        const int rg = N1 - gc + g - 1, ri = N1 - gc - g + 1 - 1;
+        at(d, 0, lg, j) = at(d, 0, li, j); at(d, 1, lg, j) = -at(d, 1, li, j); at(d, 2, lg, j) = at(d, 2, li, j);
+        at(d, 0, rg, j) = at(d, 0, ri, j); at(d, 1, rg, j) = -at(d, 1, ri, j); at(d, 2, rg, j) = at(d, 2, ri, j);
+      }
+    }
+    // Y: ghost rows at interior columns.
+    for (int g = 1; g <= gc; ++g) {
+      const int lg = g - 1, li = 2 * gc + 1 - g - 1;
+      const int rg = N2 - gc + g - 1, ri = N2 - gc - g + 1 - 1;
+      for (int i = gc; i < gc + s.p.nx; ++i) {
+        at(d, 0, i, lg) = at(d, 0, i, li); at(d, 1, i, lg) = at(d, 1, i, li); at(d, 2, i, lg) = -at(d, 2, i, li);
+        at(d, 0, i, rg) = at(d, 0, i, ri); at(d, 1, i, rg) = at(d, 1, i, ri); at(d, 2, i, rg) = -at(d, 2, i, ri);
+      }
+    }
+  }
+
+  // --- src/timestepper/rungekutta.jl:26-52, forwardeuler.jl:28-47 ----------
+  double do_substep(int s_idx, double dt, double max_dt) {
+    std::vector<T>& out = s.U[s_idx + 1];
+    const std::vector<T>& cur = s.U[s_idx];
+    std::fill(out.begin(), out.end(), (T)0);
+    T speed[2];
+    add_time_derivative(out, cur, speed);
+    if (s_idx == 0) {
+      // timestep_computer, src/simulator.jl:147-150
+      const double dxs = s.dx / (double)speed[0];
+      const double dys = s.dy / (double)speed[1];
+      dt = jl_min<double>((double)s.cfl * jl_min<double>(dxs, dys), max_dt);
+      if (sizeof(T) == 4) dt = (double)(float)dt;  // MVector{1,Float32} storage
+    }
+    const T tdt = (T)dt;
+    const size_t n = 3 * s.plane;
+#pragma omp parallel for schedule(static)
+    for (long long c = 0; c < (long long)n; ++c) out[c] = cur[c] + tdt * out[c];
+    if (s.p.stepper == VFO_STEPPER_RK2 && s_idx == 1) {
+      const std::vector<T>& first = s.U[0];
+#pragma omp parallel for schedule(static)
+      for (long long c = 0; c < (long long)n; ++c) out[c] = (T)0.5 * (first[c] + out[c]);
+    }
+    return dt;
+  }
+
+  // --- src/simulator.jl:145-177 --------------------------------------------
+  double perform_step(double max_dt) {
+    const int nsub = s.p.stepper == VFO_STEPPER_RK2 ? 2 : 1;
+    for (int st = 0; st < nsub; ++st) {
+      s.current_dt = do_substep(st, s.current_dt, max_dt);
+      if (s.p.friction != VFO_FRICTION_NONE) implicit_friction(s.U[st + 1], s.U[st], s.current_dt);
+      post_proc(s.U[st + 1]);
+      update_bc(s.U[st + 1]);
+    }
+    std::swap(s.U[0], s.U[nsub]);
+    return s.current_dt;
+  }
+};
+
+struct Handle {
+  int real_bytes;
+  Sim<double>* d;
+  Sim<float>* f;
+};
+
+template <typename T>
+Sim<T>* make_sim(const vfo_params* p, const double* Bc) {
+  Sim<T>* s = new (std::nothrow) Sim<T>();
+  if (!s) return nullptr;
+  s->p = *p;
+  s->N1 = p->nx + 2 * p->gc;
+  s->N2 = p->ny + 2 * p->gc;
+  s->plane = (size_t)s->N1 * s->N2;
+  s->dx = (p->extent[1] - p->extent[0]) / p->nx;
+  s->dy = (p->extent[3] - p->extent[2]) / p->ny;
+  if (!p->bottom_is_constant) s->B.assign(Bc, Bc + (size_t)(s->N1 + 1) * (s->N2 + 1));
+  const int nsub = p->stepper == VFO_STEPPER_RK2 ? 2 : 1;
+  s->U.assign(nsub + 1, std::vector<T>(3 * s->plane, (T)0));
+  s->left.assign(3 * s->plane, (T)0);
+  s->right.assign(3 * s->plane, (T)0);
+  s->ws.assign(s->plane, (T)0);
+  s->t = 0;
+  s->current_dt = 0;
+  s->g = (T)p->g; s->rho = (T)p->rho; s->cutoff = (T)p->depth_cutoff; s->kappa = (T)p->desingularizing_kappa;
+  s->theta = (T)p->theta; s->cfl = (T)p->cfl;
+  return s;
+}
+
+int check_params(const vfo_params* p, const double* B) {
+  if (!p) return -1;
+  if (p->nx < 2 || p->ny < 2 || p->gc < 2) return -1;
+  if (p->real_bytes != 8 && p->real_bytes != 4) return -1;
+  if (p->stepper != VFO_STEPPER_FE && p->stepper != VFO_STEPPER_RK2) return -1;
+  if (p->bc != VFO_BC_WALL || p->reconstruction != VFO_REC_LINEAR) return -1;
+  if (p->n_sources < 0 || p->n_sources > VFO_MAX_SOURCES) return -1;
+  if (!p->bottom_is_constant && !B) return -1;
+  return 0;
+}
+
+template <typename T>
+void set_interior(Sim<T>* s, const double* w, const double* hu, const double* hv) {
+  const double* src[3] = {w, hu, hv};
+  const int gc = s->p.gc;
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < s->p.ny; ++j)
+      for (int i = 0; i < s->p.nx; ++i)
+        s->U[0][(size_t)k * s->plane + s->id(i + gc, j + gc)] = (T)src[k][(size_t)i + (size_t)s->p.nx * j];
+  Ops<T>(*s).update_bc(s->U[0]);
+}
+
+template <typename T>
+void get_interior(const Sim<T>* s, double* w, double* hu, double* hv) {
+  double* dst[3] = {w, hu, hv};
+  const int gc = s->p.gc;
+  for (int k = 0; k < 3; ++k)
+    for (int j = 0; j < s->p.ny; ++j)
+      for (int i = 0; i < s->p.nx; ++i)
+        dst[k][(size_t)i + (size_t)s->p.nx * j] = (double)s->U[0][(size_t)k * s->plane + s->id(i + gc, j + gc)];
+}
+
+template <typename T>
+int simulate(Sim<T>* s, double endtime, int match_endtime, double maximum_timestep, long long max_steps,
+             long long* steps_out) {
+  Ops<T> ops(*s);
+  long long n = 0;
+  while (s->t < endtime) {
+    double max_dt = match_endtime ? endtime - s->t : std::numeric_limits<double>::infinity();
+    if (maximum_timestep >= 0) max_dt = jl_min<double>(max_dt, maximum_timestep);
+    ops.perform_step(max_dt);
+    if (sizeof(T) == 4)
+      s->t = (double)((float)s->t + (float)s->current_dt);
+    else
+      s->t += s->current_dt;
+    ++n;
+    if (max_steps > 0 && n >= max_steps) break;
+  }
+  if (steps_out) *steps_out = n;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vfo_create(const vfo_params* p, const double* B_corners, vfo_sim** out) {
+  if (!out || check_params(p, B_corners)) return -1;
+  Handle* h = new (std::nothrow) Handle();
+  if (!h) return -2;
+  h->real_bytes = p->real_bytes;
+  h->d = nullptr;
+  h->f = nullptr;
+  if (p->real_bytes == 8) h->d = make_sim<double>(p, B_corners);
+  else h->f = make_sim<float>(p, B_corners);
+  if (!h->d && !h->f) { delete h; return -2; }
+  *out = reinterpret_cast<vfo_sim*>(h);
+  return 0;
+}
+
+void vfo_destroy(vfo_sim* s) {
+  Handle* h = reinterpret_cast<Handle*>(s);
+  if (!h) return;
+  delete h->d;
+  delete h->f;
+  delete h;
+}
+
+int vfo_set_interior(vfo_sim* s, const double* w, const double* hu, const double* hv) {
+  Handle* h = reinterpret_cast<Handle*>(s);
+  if (!h || !w || !hu || !hv) return -1;
+  if (h->d) set_interior(h->d, w, hu, hv); else set_interior(h->f, w, hu, hv);
+  return 0;
+}
+
+int vfo_get_state(const vfo_sim* s, double* out) {
+  const Handle* h = reinterpret_cast<const Handle*>(s);
+  if (!h || !out) return -1;
+  if (h->d) { std::memcpy(out, h->d->U[0].data(), 3 * h->d->plane * sizeof(double)); return 0; }
+  for (size_t c = 0; c < 3 * h->f->plane; ++c) out[c] = (double)h->f->U[0][c];
+  return 0;
+}
+
+int vfo_get_interior(const vfo_sim* s, double* w, double* hu, double* hv) {
+  const Handle* h = reinterpret_cast<const Handle*>(s);
+  if (!h || !w || !hu || !hv) return -1;
+  if (h->d) get_interior(h->d, w, hu, hv); else get_interior(h->f, w, hu, hv);
+  return 0;
+}
+
+int vfo_perform_step(vfo_sim* s, double max_dt, double* dt_out) {
+  Handle* h = reinterpret_cast<Handle*>(s);
+  if (!h) return -1;
+  double dt = h->d ? Ops<double>(*h->d).perform_step(max_dt) : Ops<float>(*h->f).perform_step(max_dt);
+  if (dt_out) *dt_out = dt;
+  return 0;
+}
+
+int vfo_simulate_to_time(vfo_sim* s, double endtime, int match_endtime, double maximum_timestep,
+                         long long max_steps, long long* steps_out) {
+  Handle* h = reinterpret_cast<Handle*>(s);
+  if (!h) return -1;
+  return h->d ? simulate(h->d, endtime, match_endtime, maximum_timestep, max_steps, steps_out)
+              : simulate(h->f, endtime, match_endtime, maximum_timestep, max_steps, steps_out);
+}
+
+double vfo_time(const vfo_sim* s) {
+  const Handle* h = reinterpret_cast<const Handle*>(s);
+  return h->d ? h->d->t : h->f->t;
+}
+
+void vfo_set_time(vfo_sim* s, double t) {
+  Handle* h = reinterpret_cast<Handle*>(s);
+  if (h->d) h->d->t = t; else h->f->t = t;
+}
+
+double vfo_current_timestep(const vfo_sim* s) {
+  const Handle* h = reinterpret_cast<const Handle*>(s);
+  return h->d ? h->d->current_dt : h->f->current_dt;
+}
+
+int vfo_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
+int vfo_get_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+double vfo_minmod(double a, double b, double c) { return Ops<double>::minmod(a, b, c); }
+double vfo_minmod_slope(double l, double c, double r, double theta) {
+  return Ops<double>::minmod_slope(l, c, r, theta);
+}
+
+double vfo_bottom_lookup(const double* B, int n1p1, int n2p1, int i, int j, int which) {
+  (void)n2p1;
+  const int W = n1p1;
+  const int x = i - 1, y = j - 1;  // reference indices are 1-based
+  switch (which) {
+    case 0: return 0.25 * (B[x + W * y] + B[x + 1 + W * y] + B[x + W * (y + 1)] + B[x + 1 + W * (y + 1)]);
+    case 1: return 0.5 * (B[x + W * y] + B[x + W * (y + 1)]);
+    case 2: return 0.5 * (B[x + 1 + W * y] + B[x + 1 + W * (y + 1)]);
+    case 3: return 0.5 * (B[x + W * y] + B[x + 1 + W * y]);
+    case 4: return 0.5 * (B[x + W * (y + 1)] + B[x + 1 + W * (y + 1)]);
+    default: return std::numeric_limits<double>::quiet_NaN();
+  }
+}
+
+int vfo_update_bc_wall(double* state, int nx, int ny, int gc) {
+  if (!state || nx < gc || ny < gc || gc < 1) return -1;
+  Sim<double> s;
+  std::memset(&s.p, 0, sizeof(s.p));
+  s.p.nx = nx; s.p.ny = ny; s.p.gc = gc;
+  s.N1 = nx + 2 * gc; s.N2 = ny + 2 * gc;
+  s.plane = (size_t)s.N1 * s.N2;
+  std::vector<double> d(state, state + 3 * s.plane);
+  Ops<double>(s).update_bc(d);
+  std::memcpy(state, d.data(), 3 * s.plane * sizeof(double));
+  return 0;
+}
+
+double vfo_cbrt(double x) { return cr_cbrt(x); }
+
+double vfo_desingularize(double h, double kappa) {
+  Sim<double> s;
+  s.kappa = kappa;
+  return Ops<double>(s).desing(h);
+}
+
+}  // extern "C"

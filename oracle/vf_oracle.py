@@ -1,0 +1,170 @@
+"""ctypes wrapper of the CPU oracle (oracle/vf_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the CPU
+baseline of bench.py, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libvforacle.so"
+
+SRC_BOTTOM, SRC_CONST_RAIN, SRC_CONST_INFIL = 1, 2, 3
+FRICTION_NONE, FRICTION_BSA2012, FRICTION_FCG2016, FRICTION_BH2021 = 0, 1, 2, 3
+STEPPER_FE, STEPPER_RK2 = 1, 2
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("gc", C.c_int),
+        ("extent", C.c_double * 4),
+        ("real_bytes", C.c_int),
+        ("g", C.c_double), ("rho", C.c_double), ("depth_cutoff", C.c_double), ("desingularizing_kappa", C.c_double),
+        ("reconstruction", C.c_int), ("theta", C.c_double),
+        ("n_sources", C.c_int), ("source_kind", C.c_int * 8), ("source_rate", C.c_double * 8),
+        ("friction", C.c_int), ("friction_Cz", C.c_double),
+        ("stepper", C.c_int), ("bc", C.c_int), ("cfl", C.c_double),
+        ("bottom_is_constant", C.c_int), ("bottom_constant", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("_vf_oracle_build", HERE / "build.py")
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    lib = C.CDLL(os.fspath(LIB_PATH))
+    P = C.c_void_p
+    D = C.c_double
+    sig = {
+        "vfo_create": (C.c_int, [C.POINTER(Params), P, C.POINTER(C.c_void_p)]),
+        "vfo_destroy": (None, [P]),
+        "vfo_set_interior": (C.c_int, [P, P, P, P]),
+        "vfo_get_state": (C.c_int, [P, P]),
+        "vfo_get_interior": (C.c_int, [P, P, P, P]),
+        "vfo_perform_step": (C.c_int, [P, D, C.POINTER(D)]),
+        "vfo_simulate_to_time": (C.c_int, [P, D, C.c_int, D, C.c_longlong, C.POINTER(C.c_longlong)]),
+        "vfo_time": (D, [P]),
+        "vfo_set_time": (None, [P, D]),
+        "vfo_current_timestep": (D, [P]),
+        "vfo_set_threads": (C.c_int, [C.c_int]),
+        "vfo_get_threads": (C.c_int, []),
+        "vfo_minmod": (D, [D, D, D]),
+        "vfo_minmod_slope": (D, [D, D, D, D]),
+        "vfo_bottom_lookup": (D, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+        "vfo_update_bc_wall": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
+        "vfo_cbrt": (D, [D]),
+        "vfo_desingularize": (D, [D, D]),
+    }
+    for n, (r, a) in sig.items():
+        f = getattr(lib, n)
+        f.restype = r
+        f.argtypes = a
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+class OracleSim:
+    """One oracle simulation; arrays use the reference's (nx, ny) [i, j] indexing."""
+
+    def __init__(self, *, nx, ny, extent=((0.0, 1.0), (0.0, 1.0)), real_bytes=8, g=9.81, rho=1.0,
+                 depth_cutoff=1e-5, desingularizing_kappa=1e-5, theta=1.2, sources=(), friction=FRICTION_NONE,
+                 friction_Cz=0.0, stepper=STEPPER_RK2, cfl=0.25, B=None, bottom_constant=0.0, gc=2):
+        self.lib = load()
+        p = Params()
+        p.nx, p.ny, p.gc = nx, ny, gc
+        e = np.asarray(extent, dtype=np.float64).reshape(-1)
+        for i in range(4):
+            p.extent[i] = e[i]
+        p.real_bytes = real_bytes
+        p.g, p.rho, p.depth_cutoff, p.desingularizing_kappa = g, rho, depth_cutoff, desingularizing_kappa
+        p.reconstruction, p.theta = 1, theta
+        p.n_sources = len(sources)
+        for i, (k, r) in enumerate(sources):
+            p.source_kind[i], p.source_rate[i] = k, r
+        p.friction, p.friction_Cz = friction, friction_Cz
+        p.stepper, p.bc, p.cfl = stepper, 1, cfl
+        self.nx, self.ny, self.gc = nx, ny, gc
+        self.N1, self.N2 = nx + 2 * gc, ny + 2 * gc
+        if B is None:
+            p.bottom_is_constant, p.bottom_constant = 1, bottom_constant
+            bptr = None
+        else:
+            B = np.asarray(B, dtype=np.float64)
+            assert B.shape == (self.N1 + 1, self.N2 + 1)
+            self._B = np.ascontiguousarray(B.T)
+            p.bottom_is_constant = 0
+            bptr = _p(self._B)
+        h = C.c_void_p()
+        rc = self.lib.vfo_create(C.byref(p), bptr, C.byref(h))
+        if rc != 0:
+            raise ValueError(f"oracle rejected the configuration ({rc})")
+        self.h = h
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.vfo_destroy(self.h)
+        except Exception:
+            pass
+
+    def set_interior(self, w, hu, hv):
+        planes = [np.ascontiguousarray(np.asarray(a, dtype=np.float64).T) for a in (w, hu, hv)]
+        assert all(pl.shape == (self.ny, self.nx) for pl in planes)
+        assert self.lib.vfo_set_interior(self.h, *(_p(pl) for pl in planes)) == 0
+
+    def interior(self):
+        planes = [np.empty((self.ny, self.nx)) for _ in range(3)]
+        assert self.lib.vfo_get_interior(self.h, *(_p(pl) for pl in planes)) == 0
+        return tuple(pl.T for pl in planes)
+
+    def state(self):
+        buf = np.empty(3 * self.N1 * self.N2)
+        assert self.lib.vfo_get_state(self.h, _p(buf)) == 0
+        p = buf.reshape(3, self.N2, self.N1)
+        return tuple(x.T for x in p)
+
+    def perform_step(self, max_dt):
+        dt = C.c_double()
+        assert self.lib.vfo_perform_step(self.h, float(max_dt), C.byref(dt)) == 0
+        return dt.value
+
+    def simulate_to_time(self, endtime, match_endtime=True, maximum_timestep=None, max_steps=0):
+        n = C.c_longlong()
+        mts = -1.0 if maximum_timestep is None else float(maximum_timestep)
+        assert self.lib.vfo_simulate_to_time(self.h, float(endtime), int(match_endtime), mts, int(max_steps),
+                                             C.byref(n)) == 0
+        return n.value
+
+    @property
+    def t(self):
+        return self.lib.vfo_time(self.h)
+
+    @t.setter
+    def t(self, v):
+        self.lib.vfo_set_time(self.h, float(v))
+
+    @property
+    def current_timestep(self):
+        return self.lib.vfo_current_timestep(self.h)
+
+
+def set_threads(n: int) -> int:
+    return load().vfo_set_threads(int(n))

@@ -1,0 +1,501 @@
+// vf_abi.cu -- the extern "C" boundary declared in include/volumefluxes_sm103.h.
+//
+// Owns device memory and the stream of each handle, converts between the
+// reference's dense Volume layout and the padded device layout, and drives the
+// step kernels (vf_launch.cuh). No CPU fallback exists: every compute entry
+// point runs on the GPU or returns an error.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <string>
+
+#include "../../include/volumefluxes_sm103.h"
+#include "vf_launch.cuh"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
+
+}  // namespace
+
+struct vf_handle {
+  vf_config cfg;
+  int device = 0;
+  size_t elem = 8;
+  cudaStream_t stream = nullptr;
+  int N1 = 0, N2 = 0;
+  long long P = 0, PS = 0, PB = 0;
+  void* U[2] = {nullptr, nullptr};
+  void* L = nullptr;
+  void* S = nullptr;
+  void* B = nullptr;
+  vf::StepRecord* rec = nullptr;
+  vf::StepRecord* rec_h = nullptr;
+  double* partial = nullptr;
+  double* vol_out = nullptr;
+  int vol_blocks = 0;
+  vf::StepArgs<double> ad;
+  vf::StepArgs<float> af;
+  bool have_state = false;
+  bool have_bottom = false;
+  std::string err;
+  long long launches = 0;
+};
+
+namespace {
+
+int fail(vf_handle* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+int cuda_fail(vf_handle* h, cudaError_t e, const char* what) {
+  return fail(h, VF_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define VF_CK(h, call)                                          \
+  do {                                                          \
+    cudaError_t e_ = (call);                                    \
+    if (e_ != cudaSuccess) return cuda_fail((h), e_, #call);    \
+  } while (0)
+
+template <typename T>
+void fill_geom(const vf_handle* h, vf::Geom<T>& g) {
+  g.nx = h->cfg.nx;
+  g.ny = h->cfg.ny;
+  g.gc = h->cfg.gc;
+  g.N1 = h->N1;
+  g.N2 = h->N2;
+  g.P = h->P;
+  g.PS = h->PS;
+  g.PB = h->PB;
+  g.bottom_const = h->cfg.bottom_is_constant;
+  g.bconst = (T)h->cfg.bottom_constant;
+  g.dx = (h->cfg.extent[1] - h->cfg.extent[0]) / h->cfg.nx;
+  g.dy = (h->cfg.extent[3] - h->cfg.extent[2]) / h->cfg.ny;
+  // Simulator.cfl is stored in the backend's real type (src/simulator.jl:68).
+  g.cfl = (double)(T)h->cfg.cfl;
+}
+
+template <typename T>
+void fill_phys(const vf_handle* h, vf::Phys<T>& p) {
+  const vf_config& c = h->cfg;
+  p.g = (T)c.g;
+  p.neg_g = (T)(-c.g);
+  p.rho = (T)c.rho;
+  p.c2 = (T)((0.5 * c.rho) * c.g);
+  p.cutoff = (T)c.depth_cutoff;
+  p.kappa = (T)c.desingularizing_kappa;
+  p.theta = (T)c.theta;
+  const double dx = (c.extent[1] - c.extent[0]) / c.nx;
+  const double dy = (c.extent[3] - c.extent[2]) / c.ny;
+  p.inv_dx = (T)(1 / dx);
+  p.inv_dy = (T)(1 / dy);
+  p.dx = (T)dx;
+  p.dy = (T)dy;
+  p.Cz = (T)c.friction_Cz;
+  p.friction = c.friction;
+  p.n_bottom = 0;
+  p.n_point = 0;
+  for (int i = 0; i < 8; ++i) p.point_add[i] = (T)0;
+  for (int i = 0; i < c.n_sources; ++i) {
+    if (c.source_kind[i] == VF_SRC_BOTTOM) {
+      ++p.n_bottom;
+    } else if (c.source_kind[i] == VF_SRC_CONST_RAIN) {
+      p.point_add[p.n_point++] = (T)(c.source_rate[i] / 3600);  // compute_rain, source_term_rain.jl:30
+    } else if (c.source_kind[i] == VF_SRC_CONST_INFIL) {
+      p.point_add[p.n_point++] = (T)(-c.source_rate[i]);        // x - r == x + (-r) exactly
+    }
+  }
+}
+
+int validate(const vf_config* c) {
+  if (!c) return fail(nullptr, VF_EINVAL, "config is NULL");
+  if (c->abi_version != VF_ABI_VERSION) return fail(nullptr, VF_EINVAL, "abi_version mismatch");
+  if (c->gc != 2)
+    return fail(nullptr, VF_EINVAL, "gc must be 2 (LinearReconstruction needs gc > 1; the kernels stage a 2-cell halo)");
+  if (c->nx < 2 || c->ny < 2) return fail(nullptr, VF_EINVAL, "nx and ny must be >= 2 for the wall mirror");
+  if ((long long)c->nx * c->ny > (1ll << 31)) return fail(nullptr, VF_EINVAL, "grid too large");
+  if (!(c->extent[1] > c->extent[0]) || !(c->extent[3] > c->extent[2]))
+    return fail(nullptr, VF_EINVAL, "extent must be increasing");
+  if (c->real_bytes != 8 && c->real_bytes != 4) return fail(nullptr, VF_EINVAL, "real_bytes must be 8 or 4");
+  if (c->reconstruction != VF_REC_LINEAR) return fail(nullptr, VF_EINVAL, "only LinearReconstruction is supported");
+  if (c->stepper != VF_STEPPER_FE && c->stepper != VF_STEPPER_RK2)
+    return fail(nullptr, VF_EINVAL, "stepper must be ForwardEuler or RungeKutta2");
+  if (c->bc != VF_BC_WALL) return fail(nullptr, VF_EINVAL, "only WallBC is supported");
+  if (c->friction < VF_FRICTION_NONE || c->friction > VF_FRICTION_BH2021)
+    return fail(nullptr, VF_EINVAL, "unknown friction law");
+  if (c->n_sources < 0 || c->n_sources > VF_MAX_SOURCES) return fail(nullptr, VF_EINVAL, "too many source terms");
+  bool has_bottom_source = false;
+  for (int i = 0; i < c->n_sources; ++i) {
+    const int k = c->source_kind[i];
+    if (k != VF_SRC_BOTTOM && k != VF_SRC_CONST_RAIN && k != VF_SRC_CONST_INFIL)
+      return fail(nullptr, VF_EINVAL, "unknown source term");
+    if (k == VF_SRC_BOTTOM) has_bottom_source = true;
+  }
+  // is_compatible, src/equations/equation.jl:74-84.
+  if (c->bottom_is_constant && c->bottom_constant != 0.0 && !has_bottom_source)
+    return fail(nullptr, VF_EINVAL,
+                "Found non-zero bottom topography in equation, but no corresponding source term. Did you forget to add "
+                "a source term to your system?");
+  if (!(c->cfl > 0)) return fail(nullptr, VF_EINVAL, "cfl must be positive");
+  return VF_OK;
+}
+
+void* plane(void* base, size_t elem, long long k, long long PS) {
+  return static_cast<char*>(base) + (size_t)(k * PS) * elem;
+}
+
+// Copies between a dense host plane block (x fastest) and the padded device layout.
+int copy_planes(vf_handle* h, void* dev, const void* host_src, void* host_dst, int x_first, int y_first, int w, int hgt,
+                int planes, const void* const* host_planes_src, void* const* host_planes_dst) {
+  const size_t e = h->elem;
+  for (int k = 0; k < planes; ++k) {
+    char* d = static_cast<char*>(plane(dev, e, k, h->PS)) + (size_t)((long long)y_first * h->P + x_first + vf::XOFF) * e;
+    if (host_src || host_planes_src) {
+      const char* s = host_planes_src ? static_cast<const char*>(host_planes_src[k])
+                                      : static_cast<const char*>(host_src) + (size_t)k * w * hgt * e;
+      if (!s) continue;
+      VF_CK(h, cudaMemcpy2DAsync(d, (size_t)h->P * e, s, (size_t)w * e, (size_t)w * e, hgt, cudaMemcpyHostToDevice,
+                                 h->stream));
+    } else {
+      char* o = host_planes_dst ? static_cast<char*>(host_planes_dst[k])
+                                : static_cast<char*>(host_dst) + (size_t)k * w * hgt * e;
+      if (!o) continue;
+      VF_CK(h, cudaMemcpy2DAsync(o, (size_t)w * e, d, (size_t)h->P * e, (size_t)w * e, hgt, cudaMemcpyDeviceToHost,
+                                 h->stream));
+    }
+  }
+  return VF_OK;
+}
+
+int launch_one_step(vf_handle* h, int k) {
+  const int parity = k & 1;
+  cudaError_t e;
+  if (h->elem == 8) {
+    e = vf::launch_step(h->ad, static_cast<const double*>(h->U[parity]), static_cast<double*>(h->U[parity ^ 1]),
+                        parity, h->stream);
+  } else {
+    e = vf::launch_step(h->af, static_cast<const float*>(h->U[parity]), static_cast<float*>(h->U[parity ^ 1]), parity,
+                        h->stream);
+  }
+  h->launches += 2;
+  if (e != cudaSuccess) return cuda_fail(h, e, "step launch");
+  return VF_OK;
+}
+
+int push_record(vf_handle* h) {
+  VF_CK(h, cudaMemcpyAsync(h->rec, h->rec_h, sizeof(vf::StepRecord), cudaMemcpyHostToDevice, h->stream));
+  return VF_OK;
+}
+
+int pull_record(vf_handle* h) {
+  VF_CK(h, cudaMemcpyAsync(h->rec_h, h->rec, sizeof(vf::StepRecord), cudaMemcpyDeviceToHost, h->stream));
+  VF_CK(h, cudaStreamSynchronize(h->stream));
+  return VF_OK;
+}
+
+void reset_record(vf_handle* h) {
+  std::memset(h->rec_h, 0, sizeof(vf::StepRecord));
+  h->rec_h->stop_time = std::numeric_limits<double>::infinity();
+  h->rec_h->endtime = std::numeric_limits<double>::infinity();
+}
+
+int ensure_ready(vf_handle* h) {
+  if (!h) return VF_EINVAL;
+  if (!h->have_state) return fail(h, VF_ESTATE, "no state uploaded (call vf_set_interior_state first)");
+  if (!h->cfg.bottom_is_constant && !h->have_bottom) return fail(h, VF_ESTATE, "bottom topography not uploaded");
+  VF_CK(h, cudaSetDevice(h->device));
+  return VF_OK;
+}
+
+void destroy(vf_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFree(h->U[0]);
+  cudaFree(h->U[1]);
+  cudaFree(h->L);
+  cudaFree(h->S);
+  cudaFree(h->B);
+  cudaFree(h->rec);
+  cudaFree(h->partial);
+  cudaFree(h->vol_out);
+  if (h->rec_h) cudaFreeHost(h->rec_h);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vf_create(const vf_config* cfg, vf_handle** out) {
+  if (!out) return fail(nullptr, VF_EINVAL, "out is NULL");
+  *out = nullptr;
+  int rc = validate(cfg);
+  if (rc) return rc;
+  vf_handle* h = new (std::nothrow) vf_handle();
+  if (!h) return fail(nullptr, VF_ENOMEM, "host allocation failed");
+  h->cfg = *cfg;
+  h->device = cfg->device;
+  h->elem = (size_t)cfg->real_bytes;
+  h->N1 = cfg->nx + 2 * cfg->gc;
+  h->N2 = cfg->ny + 2 * cfg->gc;
+  // Rows padded to 32 elements with XOFF leading columns so interior rows start
+  // 16-byte aligned; planes padded to whole rows of 32 elements.
+  h->P = round_up(vf::XOFF + h->N1, 32);
+  h->PS = h->P * h->N2;
+  h->PB = round_up(vf::XOFF + h->N1 + 1, 32);
+  cudaError_t e = cudaSetDevice(h->device);
+  if (e != cudaSuccess) {
+    delete h;
+    return cuda_fail(nullptr, e, "cudaSetDevice");
+  }
+  e = h->elem == 8 ? vf::configure_kernels_f64() : vf::configure_kernels_f32();
+  if (e != cudaSuccess) {
+    delete h;
+    return cuda_fail(nullptr, e, "kernel configuration");
+  }
+  const size_t state_bytes = (size_t)(3 * h->PS) * h->elem;
+  bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->U[0], state_bytes) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->U[1], state_bytes) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->L, state_bytes) == cudaSuccess;
+  if (cfg->friction != VF_FRICTION_NONE) ok = ok && cudaMalloc(&h->S, (size_t)h->PS * h->elem) == cudaSuccess;
+  if (!cfg->bottom_is_constant)
+    ok = ok && cudaMalloc(&h->B, (size_t)(h->PB * (h->N2 + 1)) * h->elem) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->rec, sizeof(vf::StepRecord)) == cudaSuccess;
+  ok = ok && cudaMallocHost(&h->rec_h, sizeof(vf::StepRecord)) == cudaSuccess;
+  h->vol_blocks = 1024;
+  ok = ok && cudaMalloc(&h->partial, sizeof(double) * h->vol_blocks) == cudaSuccess;
+  ok = ok && cudaMalloc(&h->vol_out, sizeof(double)) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    destroy(h);
+    return fail(nullptr, VF_ENOMEM, "device allocation failed");
+  }
+  ok = cudaMemsetAsync(h->U[0], 0, state_bytes, h->stream) == cudaSuccess;
+  ok = ok && cudaMemsetAsync(h->U[1], 0, state_bytes, h->stream) == cudaSuccess;
+  ok = ok && cudaMemsetAsync(h->L, 0, state_bytes, h->stream) == cudaSuccess;
+  if (h->S) ok = ok && cudaMemsetAsync(h->S, 0, (size_t)h->PS * h->elem, h->stream) == cudaSuccess;
+  if (h->B) ok = ok && cudaMemsetAsync(h->B, 0, (size_t)(h->PB * (h->N2 + 1)) * h->elem, h->stream) == cudaSuccess;
+  ok = ok && cudaMemsetAsync(h->rec, 0, sizeof(vf::StepRecord), h->stream) == cudaSuccess;
+  ok = ok && cudaStreamSynchronize(h->stream) == cudaSuccess;
+  if (!ok) {
+    cudaError_t le = cudaGetLastError();
+    destroy(h);
+    return cuda_fail(nullptr, le, "device initialisation");
+  }
+  fill_geom(h, h->ad.g);
+  fill_phys(h, h->ad.p);
+  fill_geom(h, h->af.g);
+  fill_phys(h, h->af.p);
+  h->ad.rk2 = h->af.rk2 = cfg->stepper == VF_STEPPER_RK2;
+  h->ad.B = static_cast<const double*>(h->B);
+  h->ad.L = static_cast<double*>(h->L);
+  h->ad.S = static_cast<double*>(h->S);
+  h->ad.rec = h->rec;
+  h->af.B = static_cast<const float*>(h->B);
+  h->af.L = static_cast<float*>(h->L);
+  h->af.S = static_cast<float*>(h->S);
+  h->af.rec = h->rec;
+  *out = h;
+  return VF_OK;
+}
+
+void vf_destroy(vf_handle* h) { destroy(h); }
+
+int vf_upload_bottom(vf_handle* h, const void* B_corners) {
+  if (!h || !B_corners) return fail(h, VF_EINVAL, "NULL argument");
+  if (h->cfg.bottom_is_constant) return fail(h, VF_EINVAL, "handle uses a ConstantBottomTopography");
+  const long long W = h->N1 + 1, H = h->N2 + 1;
+  // is_compatible, src/equations/equation.jl:74-84: non-zero B needs SourceTermBottom.
+  bool has_bottom_source = false;
+  for (int i = 0; i < h->cfg.n_sources; ++i) has_bottom_source |= h->cfg.source_kind[i] == VF_SRC_BOTTOM;
+  if (!has_bottom_source) {
+    for (long long n = 0; n < W * H; ++n) {
+      const double v = h->elem == 8 ? static_cast<const double*>(B_corners)[n] : static_cast<const float*>(B_corners)[n];
+      if (v != 0.0)
+        return fail(h, VF_EINVAL,
+                    "Found non-zero bottom topography in equation, but no corresponding source term. Did you forget to "
+                    "add a source term to your system?");
+    }
+  }
+  VF_CK(h, cudaSetDevice(h->device));
+  char* d = static_cast<char*>(h->B) + (size_t)vf::XOFF * h->elem;
+  VF_CK(h, cudaMemcpy2DAsync(d, (size_t)h->PB * h->elem, B_corners, (size_t)W * h->elem, (size_t)W * h->elem, H,
+                             cudaMemcpyHostToDevice, h->stream));
+  VF_CK(h, cudaStreamSynchronize(h->stream));
+  h->have_bottom = true;
+  return VF_OK;
+}
+
+int vf_set_interior_state(vf_handle* h, const void* w, const void* hu, const void* hv) {
+  if (!h || !w || !hu || !hv) return fail(h, VF_EINVAL, "NULL argument");
+  VF_CK(h, cudaSetDevice(h->device));
+  const void* planes[3] = {w, hu, hv};
+  int rc = copy_planes(h, h->U[0], nullptr, nullptr, h->cfg.gc, h->cfg.gc, h->cfg.nx, h->cfg.ny, 3, planes, nullptr);
+  if (rc) return rc;
+  cudaError_t e = h->elem == 8 ? vf::launch_bc(h->ad.g, static_cast<double*>(h->U[0]), h->stream)
+                               : vf::launch_bc(h->af.g, static_cast<float*>(h->U[0]), h->stream);
+  h->launches += 1;
+  if (e != cudaSuccess) return cuda_fail(h, e, "boundary update");
+  VF_CK(h, cudaStreamSynchronize(h->stream));
+  h->have_state = true;
+  return VF_OK;
+}
+
+int vf_upload_state(vf_handle* h, const void* state) {
+  if (!h || !state) return fail(h, VF_EINVAL, "NULL argument");
+  VF_CK(h, cudaSetDevice(h->device));
+  int rc = copy_planes(h, h->U[0], state, nullptr, 0, 0, h->N1, h->N2, 3, nullptr, nullptr);
+  if (rc) return rc;
+  VF_CK(h, cudaStreamSynchronize(h->stream));
+  h->have_state = true;
+  return VF_OK;
+}
+
+int vf_download_state(vf_handle* h, void* state) {
+  if (!h || !state) return fail(h, VF_EINVAL, "NULL argument");
+  VF_CK(h, cudaSetDevice(h->device));
+  int rc = copy_planes(h, h->U[0], nullptr, state, 0, 0, h->N1, h->N2, 3, nullptr, nullptr);
+  if (rc) return rc;
+  VF_CK(h, cudaStreamSynchronize(h->stream));
+  return VF_OK;
+}
+
+int vf_get_interior_state(vf_handle* h, void* w, void* hu, void* hv) {
+  if (!h) return VF_EINVAL;
+  VF_CK(h, cudaSetDevice(h->device));
+  void* planes[3] = {w, hu, hv};
+  int rc = copy_planes(h, h->U[0], nullptr, nullptr, h->cfg.gc, h->cfg.gc, h->cfg.nx, h->cfg.ny, 3, nullptr, planes);
+  if (rc) return rc;
+  VF_CK(h, cudaStreamSynchronize(h->stream));
+  return VF_OK;
+}
+
+int vf_step(vf_handle* h, double max_dt, double* dt_out) {
+  int rc = ensure_ready(h);
+  if (rc) return rc;
+  reset_record(h);
+  h->rec_h->active[0] = 1;
+  h->rec_h->explicit_mode = 1;
+  h->rec_h->explicit_max_dt = max_dt;
+  if ((rc = push_record(h))) return rc;
+  if ((rc = launch_one_step(h, 0))) return rc;
+  if ((rc = pull_record(h))) return rc;
+  std::swap(h->U[0], h->U[1]);
+  if (dt_out) *dt_out = h->rec_h->last_dt;
+  return VF_OK;
+}
+
+int vf_simulate(vf_handle* h, double t0, double endtime, int32_t match_endtime, double maximum_timestep,
+                double stop_time, int64_t max_steps, double* t_out, int64_t* steps_out, double* last_dt_out) {
+  int rc = ensure_ready(h);
+  if (rc) return rc;
+  reset_record(h);
+  vf::StepRecord* r = h->rec_h;
+  r->t[0] = t0;
+  r->active[0] = t0 < endtime ? 1 : 0;
+  r->match_endtime = match_endtime ? 1 : 0;
+  r->has_max_ts = maximum_timestep >= 0 ? 1 : 0;
+  r->max_ts = maximum_timestep;
+  r->endtime = endtime;
+  r->stop_time = stop_time;
+  const bool limited = max_steps > 0;
+  if ((rc = push_record(h))) return rc;
+  long long k = 0;
+  long long chunk = 8;
+  if (r->active[0]) {
+    for (;;) {
+      long long n = chunk;
+      if (limited && k + n > max_steps) n = max_steps - k;
+      for (long long i = 0; i < n; ++i)
+        if ((rc = launch_one_step(h, (int)((k + i) & 1)))) return rc;
+      k += n;
+      if ((rc = pull_record(h))) return rc;
+      if (!h->rec_h->active[k & 1]) break;
+      if (limited && k >= max_steps) break;
+      if (chunk < 256) chunk *= 2;
+    }
+  }
+  if (k == 0 && (rc = pull_record(h))) return rc;
+  const long long done = h->rec_h->n_done;
+  if (done & 1) std::swap(h->U[0], h->U[1]);
+  if (t_out) *t_out = h->rec_h->t[k & 1];
+  if (steps_out) *steps_out = done;
+  if (last_dt_out) *last_dt_out = h->rec_h->last_dt;
+  return VF_OK;
+}
+
+int vf_time_steps(vf_handle* h, int64_t n_steps, float* ms_out) {
+  int rc = ensure_ready(h);
+  if (rc) return rc;
+  if (n_steps < 1) return fail(h, VF_EINVAL, "n_steps must be >= 1");
+  reset_record(h);
+  h->rec_h->active[0] = 1;
+  h->rec_h->t[0] = 0.0;
+  if ((rc = push_record(h))) return rc;
+  cudaEvent_t e0, e1;
+  VF_CK(h, cudaEventCreate(&e0));
+  VF_CK(h, cudaEventCreate(&e1));
+  VF_CK(h, cudaEventRecord(e0, h->stream));
+  for (long long k = 0; k < n_steps; ++k)
+    if ((rc = launch_one_step(h, (int)(k & 1)))) return rc;
+  VF_CK(h, cudaEventRecord(e1, h->stream));
+  VF_CK(h, cudaEventSynchronize(e1));
+  float ms = 0.f;
+  VF_CK(h, cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if ((rc = pull_record(h))) return rc;
+  if (h->rec_h->n_done & 1) std::swap(h->U[0], h->U[1]);
+  if (ms_out) *ms_out = ms;
+  return VF_OK;
+}
+
+int vf_water_volume(vf_handle* h, double* out) {
+  int rc = ensure_ready(h);
+  if (rc) return rc;
+  if (!out) return fail(h, VF_EINVAL, "NULL argument");
+  cudaError_t e = h->elem == 8
+                      ? vf::launch_volume(h->ad.g, static_cast<const double*>(h->U[0]),
+                                          static_cast<const double*>(h->B), h->partial, h->vol_blocks, h->vol_out,
+                                          h->stream)
+                      : vf::launch_volume(h->af.g, static_cast<const float*>(h->U[0]), static_cast<const float*>(h->B),
+                                          h->partial, h->vol_blocks, h->vol_out, h->stream);
+  h->launches += 2;
+  if (e != cudaSuccess) return cuda_fail(h, e, "volume launch");
+  VF_CK(h, cudaMemcpyAsync(out, h->vol_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  VF_CK(h, cudaStreamSynchronize(h->stream));
+  return VF_OK;
+}
+
+int vf_device_state(vf_handle* h, void** base, int64_t* pitch, int64_t* plane_stride, int64_t* offset00) {
+  if (!h) return VF_EINVAL;
+  if (base) *base = h->U[0];
+  if (pitch) *pitch = h->P;
+  if (plane_stride) *plane_stride = h->PS;
+  if (offset00) *offset00 = vf::XOFF;
+  return VF_OK;
+}
+
+int vf_stream(vf_handle* h, void** stream) {
+  if (!h || !stream) return VF_EINVAL;
+  *stream = h->stream;
+  return VF_OK;
+}
+
+const char* vf_last_error(vf_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int64_t vf_launch_count(vf_handle* h) { return h ? h->launches : 0; }
+
+}  // extern "C"

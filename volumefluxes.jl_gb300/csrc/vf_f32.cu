@@ -1,0 +1,15 @@
+// vf_f32.cu -- Float32 step kernels (multiply-add contraction and fast
+// division allowed; the error is stated against the Float64 oracle).
+#include "vf_step_impl.cuh"
+
+namespace vf {
+cudaError_t launch_step(const StepArgs<float>& a, const float* Uin, float* Uout, int parity, cudaStream_t st) {
+  return launch_step_impl<float>(a, Uin, Uout, parity, st);
+}
+cudaError_t launch_bc(const Geom<float>& g, float* U, cudaStream_t st) { return launch_bc_impl<float>(g, U, st); }
+cudaError_t launch_volume(const Geom<float>& g, const float* U, const float* B, double* partial, int nblocks,
+                          double* out, cudaStream_t st) {
+  return launch_volume_impl<float>(g, U, B, partial, nblocks, out, st);
+}
+cudaError_t configure_kernels_f32() { return configure_impl<float>(); }
+}  // namespace vf

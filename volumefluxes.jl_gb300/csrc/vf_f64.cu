@@ -1,0 +1,16 @@
+// vf_f64.cu -- Float64 step kernels. Built with -fmad=false: no multiply-add
+// contraction, IEEE division and square root, so each operation rounds as the
+// reference's Julia code does.
+#include "vf_step_impl.cuh"
+
+namespace vf {
+cudaError_t launch_step(const StepArgs<double>& a, const double* Uin, double* Uout, int parity, cudaStream_t st) {
+  return launch_step_impl<double>(a, Uin, Uout, parity, st);
+}
+cudaError_t launch_bc(const Geom<double>& g, double* U, cudaStream_t st) { return launch_bc_impl<double>(g, U, st); }
+cudaError_t launch_volume(const Geom<double>& g, const double* U, const double* B, double* partial, int nblocks,
+                          double* out, cudaStream_t st) {
+  return launch_volume_impl<double>(g, U, B, partial, nblocks, out, st);
+}
+cudaError_t configure_kernels_f64() { return configure_impl<double>(); }
+}  // namespace vf

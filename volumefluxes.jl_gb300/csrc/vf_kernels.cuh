@@ -1,0 +1,597 @@
+// vf_kernels.cuh -- the fused tile kernels of one RK2 / forward-Euler step.
+//
+// A step is two launches (three for nothing else):
+//   flux pass   reads U0 (+2-cell halo) and B, computes the time derivative
+//               L(U0) of src/system.jl:62-75 (x then y: reconstruction, central-
+//               upwind fluxes, bottom source; then rain/infiltration), the
+//               friction factor S(U0) of src/friction.jl:62-78, and the CFL
+//               maxima (warp shuffles + one atomicMax per block per direction).
+//   stage pass  (RK2) reads U0, L, S on the tile + halo, forms the stage-1
+//               result U1 = clamp((U0 + dt*L) ./ (1 .- dt*[0,S,S])) pointwise in
+//               shared memory with its wall ghosts, runs the whole stage-2
+//               derivative on U1, then the Euler update, RK2 average, friction,
+//               dry clamp and wall ghosts of U2 (src/timestepper/rungekutta.jl:26-52,
+//               src/simulator.jl:145-177). dt comes from the flux pass's maxima
+//               (src/simulator.jl:147-150) and is computed on the device.
+//   apply pass  (forward Euler) the pointwise stage-1 update alone.
+//
+// Tiles are TX x TY interior cells; each block stages its tile with a 2-cell
+// halo of (w, hu, hv) and a 2..3-cell halo of bottom corners in shared memory.
+#pragma once
+#include "vf_math.cuh"
+
+namespace vf {
+
+constexpr int TX = 32;
+constexpr int TY = 16;
+constexpr int NT = 256;
+constexpr int CPT = TX * TY / NT;  // cells per thread
+constexpr int HX = TX + 4;
+constexpr int HY = TY + 4;
+constexpr int BHX = TX + 5;
+constexpr int BHY = TY + 5;
+constexpr int LRN = (TX + 2) * TY > TX * (TY + 2) ? (TX + 2) * TY : TX * (TY + 2);
+constexpr int FN = (TX + 1) * TY > TX * (TY + 1) ? (TX + 1) * TY : TX * (TY + 1);
+constexpr int XOFF = 2;  // leading pad columns in device rows
+
+// Device-resident step record. Slots indexed by step parity let every kernel
+// of step n read slot n&1 while the stage pass prepares slot (n+1)&1.
+struct StepRecord {
+  unsigned long long speed_bits[2][2];  // CFL maxima (ax, ay) as IEEE bit patterns, >= 0
+  double t[2];
+  int active[2];
+  int match_endtime;
+  int has_max_ts;
+  double endtime;
+  double max_ts;
+  double stop_time;
+  double last_dt;
+  long long n_done;
+  double explicit_max_dt;
+  int explicit_mode;
+  int pad_;
+};
+
+template <typename T>
+struct Geom {
+  int nx, ny, gc, N1, N2;
+  long long P, PS, PB;  // state row pitch, plane stride, corner row pitch (elements)
+  int bottom_const;
+  T bconst;
+  double dx, dy, cfl;
+};
+
+template <typename T>
+__device__ __forceinline__ long long sidx(const Geom<T>& g, int x, int y) {
+  return (long long)y * g.P + x + XOFF;
+}
+
+// Bottom topography seen from a tile; (lx, ly) are tile-local cell coordinates,
+// corner (x0+lx, y0+ly) lives at sB[(ly+2)*BHX + lx+2]. Lookups follow
+// src/bottom_topography.jl:97-101.
+template <typename T>
+struct BTile {
+  const T* sB;
+  int is_const;
+  T c;
+  __device__ __forceinline__ T cn(int lx, int ly) const { return sB[(ly + 2) * BHX + lx + 2]; }
+  __device__ __forceinline__ T cell(int lx, int ly) const {
+    if (is_const) return c;
+    return (T)0.25 * (((cn(lx, ly) + cn(lx + 1, ly)) + cn(lx, ly + 1)) + cn(lx + 1, ly + 1));
+  }
+  template <int DIR>
+  __device__ __forceinline__ T face_l(int lx, int ly) const {
+    if (is_const) return c;
+    return DIR == 0 ? (T)0.5 * (cn(lx, ly) + cn(lx, ly + 1)) : (T)0.5 * (cn(lx, ly) + cn(lx + 1, ly));
+  }
+  template <int DIR>
+  __device__ __forceinline__ T face_r(int lx, int ly) const {
+    if (is_const) return c;
+    return DIR == 0 ? (T)0.5 * (cn(lx + 1, ly) + cn(lx + 1, ly + 1)) : (T)0.5 * (cn(lx, ly + 1) + cn(lx + 1, ly + 1));
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ void load_corners(const Geom<T>& g, const T* __restrict__ B, T* sB, int x0, int y0) {
+  for (int idx = threadIdx.x; idx < BHX * BHY; idx += NT) {
+    const int bx = idx % BHX, by = idx / BHX;
+    const int cx = x0 - 2 + bx, cy = y0 - 2 + by;
+    T v = (T)0;
+    if (cx <= g.N1 && cy <= g.N2) v = B[(long long)cy * g.PB + cx + XOFF];
+    sB[idx] = v;
+  }
+}
+
+// Time derivative of one stage on the tile held in sU (3 planes of HY x HX).
+// acc[k][*] receives -(1/Δx)(F_r-F_l) [+ bottom x], then -(1/Δy)(G_r-G_l)
+// [+ bottom y] for the cells this thread owns (cell tid + k*NT, x fastest).
+// src/system.jl:64-70 (directions in order), numericalflux.jl:21-33,
+// linearreconstruction.jl:58-102, source_term_bottom.jl:24-41.
+template <typename T, bool SPEED>
+__device__ __forceinline__ void tile_derivative(const Phys<T>& p, const T* sU, const BTile<T>& bt, T* sL, T* sR, T* sF,
+                                                T (&acc)[CPT][3], T& mx, T& my, int nvx, int nvy) {
+  const int tid = threadIdx.x;
+  // ---- x: reconstruct cells lx in [-1, TX], ly in [0, TY)
+  for (int idx = tid; idx < (TX + 2) * TY; idx += NT) {
+    const int lx = idx % (TX + 2) - 1, ly = idx / (TX + 2);
+    const int c = (ly + 2) * HX + lx + 2;
+    T l[3], m[3], r[3], L[3], R[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      l[k] = sU[k * HX * HY + c - 1];
+      m[k] = sU[k * HX * HY + c];
+      r[k] = sU[k * HX * HY + c + 1];
+    }
+    reconstruct_cell<T>(p, l, m, r, bt.template face_l<0>(lx, ly), bt.template face_r<0>(lx, ly), L, R);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      sL[k * LRN + idx] = L[k];
+      sR[k * LRN + idx] = R[k];
+    }
+  }
+  __syncthreads();
+  // ---- x: faces f in [0, TX] between cells f-1 and f
+  for (int idx = tid; idx < (TX + 1) * TY; idx += NT) {
+    const int f = idx % (TX + 1), ly = idx / (TX + 1);
+    const int im = ly * (TX + 2) + f, ip = im + 1;
+    T F0, F1, F2, sp = (T)0;
+    cu_face<T, 0, SPEED>(p, sR[im], sR[LRN + im], sR[2 * LRN + im], sL[ip], sL[LRN + ip], sL[2 * LRN + ip], F0, F1, F2,
+                         sp);
+    sF[idx] = F0;
+    sF[FN + idx] = F1;
+    sF[2 * FN + idx] = F2;
+    if (SPEED && ly < nvy && f <= nvx) mx = fmax(mx, sp);
+  }
+  __syncthreads();
+  // ---- x: accumulate
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    const int c = tid + k * NT;
+    const int lx = c % TX, ly = c / TX;
+    const int fl = ly * (TX + 1) + lx;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) acc[k][j] = (T)0 - p.inv_dx * (sF[j * FN + fl + 1] - sF[j * FN + fl]);
+    const int rc = ly * (TX + 2) + lx + 1;
+    for (int b = 0; b < p.n_bottom; ++b) {
+      const T Bl = bt.template face_l<0>(lx, ly), Br = bt.template face_r<0>(lx, ly);
+      acc[k][1] = acc[k][1] + p.neg_g * vdiv<T>(Br - Bl, p.dx) * ((sR[rc] + sL[rc]) * (T)0.5);
+    }
+  }
+  __syncthreads();
+  // ---- y: reconstruct cells lx in [0, TX), ly in [-1, TY]
+  for (int idx = tid; idx < TX * (TY + 2); idx += NT) {
+    const int lx = idx % TX, ly = idx / TX - 1;
+    const int c = (ly + 2) * HX + lx + 2;
+    T l[3], m[3], r[3], L[3], R[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      l[k] = sU[k * HX * HY + c - HX];
+      m[k] = sU[k * HX * HY + c];
+      r[k] = sU[k * HX * HY + c + HX];
+    }
+    reconstruct_cell<T>(p, l, m, r, bt.template face_l<1>(lx, ly), bt.template face_r<1>(lx, ly), L, R);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      sL[k * LRN + idx] = L[k];
+      sR[k * LRN + idx] = R[k];
+    }
+  }
+  __syncthreads();
+  // ---- y: faces f in [0, TY] between cells f-1 and f
+  for (int idx = tid; idx < TX * (TY + 1); idx += NT) {
+    const int lx = idx % TX, f = idx / TX;
+    const int im = f * TX + lx, ip = im + TX;
+    T F0, F1, F2, sp = (T)0;
+    cu_face<T, 1, SPEED>(p, sR[im], sR[LRN + im], sR[2 * LRN + im], sL[ip], sL[LRN + ip], sL[2 * LRN + ip], F0, F1, F2,
+                         sp);
+    sF[idx] = F0;
+    sF[FN + idx] = F1;
+    sF[2 * FN + idx] = F2;
+    if (SPEED && lx < nvx && f <= nvy) my = fmax(my, sp);
+  }
+  __syncthreads();
+  // ---- y: accumulate
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    const int c = tid + k * NT;
+    const int lx = c % TX, ly = c / TX;
+    const int fl = ly * TX + lx;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) acc[k][j] = acc[k][j] - p.inv_dy * (sF[j * FN + fl + TX] - sF[j * FN + fl]);
+    const int rc = (ly + 1) * TX + lx;
+    for (int b = 0; b < p.n_bottom; ++b) {
+      const T Bl = bt.template face_l<1>(lx, ly), Br = bt.template face_r<1>(lx, ly);
+      acc[k][2] = acc[k][2] + p.neg_g * vdiv<T>(Br - Bl, p.dy) * ((sR[rc] + sL[rc]) * (T)0.5);
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ unsigned long long speed_key(T v);
+template <>
+__device__ __forceinline__ unsigned long long speed_key<double>(double v) {
+  return (unsigned long long)__double_as_longlong(v);
+}
+template <>
+__device__ __forceinline__ unsigned long long speed_key<float>(float v) {
+  return (unsigned long long)(unsigned)__float_as_uint(v);
+}
+template <typename T>
+__device__ __forceinline__ double speed_from_key(unsigned long long k);
+template <>
+__device__ __forceinline__ double speed_from_key<double>(unsigned long long k) {
+  return __longlong_as_double((long long)k);
+}
+template <>
+__device__ __forceinline__ double speed_from_key<float>(unsigned long long k) {
+  return (double)__uint_as_float((unsigned)k);
+}
+
+// ---------------------------------------------------------------------------
+// Flux pass: L(U0), S(U0) and the CFL maxima.
+template <typename T>
+struct SmemFlux {
+  T U[3 * HX * HY];
+  T B[BHX * BHY];
+  T L[3 * LRN];
+  T R[3 * LRN];
+  T F[3 * FN];
+  unsigned long long red[2][NT / 32];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_flux(Geom<T> g, Phys<T> p, const T* __restrict__ U, const T* __restrict__ B,
+                                             T* __restrict__ Lout, T* __restrict__ Sout, StepRecord* rec, int parity) {
+  if (!rec->active[parity]) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SmemFlux<T>& s = *reinterpret_cast<SmemFlux<T>*>(smem_raw);
+  const int tid = threadIdx.x;
+  const int x0 = g.gc + blockIdx.x * TX, y0 = g.gc + blockIdx.y * TY;
+  const int nvx = min(TX, g.gc + g.nx - x0), nvy = min(TY, g.gc + g.ny - y0);
+
+  for (int idx = tid; idx < HX * HY; idx += NT) {
+    const int lx = idx % HX, ly = idx / HX;
+    const int gx = x0 - 2 + lx, gy = y0 - 2 + ly;
+    const bool ok = gx < g.N1 && gy < g.N2;
+    const long long o = sidx(g, gx, gy);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) s.U[k * HX * HY + idx] = ok ? U[k * g.PS + o] : (T)0;
+  }
+  if (!g.bottom_const) load_corners(g, B, s.B, x0, y0);
+  __syncthreads();
+
+  BTile<T> bt{s.B, g.bottom_const, g.bconst};
+  T acc[CPT][3];
+  T mx = (T)0, my = (T)0;
+  tile_derivative<T, true>(p, s.U, bt, s.L, s.R, s.F, acc, mx, my, nvx, nvy);
+
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    const int c = tid + k * NT;
+    const int lx = c % TX, ly = c / TX;
+    if (lx >= nvx || ly >= nvy) continue;
+    for (int n = 0; n < p.n_point; ++n) acc[k][0] = acc[k][0] + p.point_add[n];
+    const long long o = sidx(g, x0 + lx, y0 + ly);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Lout[j * g.PS + o] = acc[k][j];
+    if (p.friction) {
+      const int ci = (ly + 2) * HX + lx + 2;
+      Sout[o] = friction_factor<T>(p, s.U[ci], s.U[HX * HY + ci], s.U[2 * HX * HY + ci], bt.cell(lx, ly));
+    }
+  }
+
+  // CFL maxima: warp shuffle, then one atomic per block and direction.
+  unsigned long long kx = speed_key<T>(mx), ky = speed_key<T>(my);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    kx = max(kx, __shfl_xor_sync(0xffffffffu, kx, o));
+    ky = max(ky, __shfl_xor_sync(0xffffffffu, ky, o));
+  }
+  if ((tid & 31) == 0) {
+    s.red[0][tid >> 5] = kx;
+    s.red[1][tid >> 5] = ky;
+  }
+  __syncthreads();
+  if (tid < 2) {
+    unsigned long long m = 0;
+    for (int w = 0; w < NT / 32; ++w) m = max(m, s.red[tid][w]);
+    atomicMax(&rec->speed_bits[parity][tid], m);
+  }
+}
+
+// dt of stage 1, src/simulator.jl:147-150, and the time bookkeeping of
+// simulate_to_time (src/simulator.jl:199-205) for the step of this parity.
+template <typename T>
+__device__ __forceinline__ double step_dt(const Geom<T>& g, const StepRecord* rec, int parity) {
+  const double ax = speed_from_key<T>(rec->speed_bits[parity][0]);
+  const double ay = speed_from_key<T>(rec->speed_bits[parity][1]);
+  double max_dt;
+  if (rec->explicit_mode) {
+    max_dt = rec->explicit_max_dt;
+  } else {
+    max_dt = rec->match_endtime ? rec->endtime - rec->t[parity] : __longlong_as_double(0x7ff0000000000000ll);
+    if (rec->has_max_ts) max_dt = jmin<double>(max_dt, rec->max_ts);
+  }
+  double dt = jmin<double>(g.cfl * jmin<double>(g.dx / ax, g.dy / ay), max_dt);
+  if (sizeof(T) == 4) dt = (double)(float)dt;  // current_timestep is a MVector{1,Float32}
+  return dt;
+}
+
+template <typename T>
+__device__ __forceinline__ void advance_record(StepRecord* rec, int parity, double dt) {
+  const double t = rec->t[parity];
+  double tn = sizeof(T) == 4 ? (double)((float)t + (float)dt) : t + dt;
+  rec->last_dt = dt;
+  rec->t[parity ^ 1] = tn;
+  rec->n_done += 1;
+  const bool more = !rec->explicit_mode && (tn < rec->endtime) && !(tn + dt >= rec->stop_time);
+  rec->active[parity ^ 1] = more ? 1 : 0;
+  rec->speed_bits[parity ^ 1][0] = 0ull;
+  rec->speed_bits[parity ^ 1][1] = 0ull;
+}
+
+__device__ __forceinline__ void carry_record(StepRecord* rec, int parity) {
+  rec->t[parity ^ 1] = rec->t[parity];
+  rec->active[parity ^ 1] = 0;
+}
+
+// Wall ghosts written by the owner of each mirror source, src/bc.jl:81-110.
+// X ghosts (interior rows) get hu negated, Y ghosts (interior columns) hv.
+template <typename T>
+__device__ __forceinline__ void store_with_ghosts(const Geom<T>& g, T* __restrict__ Uo, int gx, int gy, T w, T hu,
+                                                  T hv) {
+  const long long o = sidx(g, gx, gy);
+  Uo[o] = w;
+  Uo[g.PS + o] = hu;
+  Uo[2 * g.PS + o] = hv;
+  const int lo = g.gc, hi = g.gc + g.nx - 1;
+  int gxs[2] = {-1, -1};
+  if (gx == lo) gxs[0] = lo - 1;
+  if (gx == lo + 1) gxs[0] = lo - 2;
+  if (gx == hi) gxs[1] = hi + 1;
+  if (gx == hi - 1) gxs[1] = hi + 2;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    if (gxs[i] >= 0) {
+      const long long q = sidx(g, gxs[i], gy);
+      Uo[q] = w;
+      Uo[g.PS + q] = -hu;
+      Uo[2 * g.PS + q] = hv;
+    }
+  }
+  const int ylo = g.gc, yhi = g.gc + g.ny - 1;
+  int gys[2] = {-1, -1};
+  if (gy == ylo) gys[0] = ylo - 1;
+  if (gy == ylo + 1) gys[0] = ylo - 2;
+  if (gy == yhi) gys[1] = yhi + 1;
+  if (gy == yhi - 1) gys[1] = yhi + 2;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    if (gys[i] >= 0) {
+      const long long q = sidx(g, gx, gys[i]);
+      Uo[q] = w;
+      Uo[g.PS + q] = hu;
+      Uo[2 * g.PS + q] = -hv;
+    }
+  }
+}
+
+// Stage-1 pointwise update of one cell: Euler, friction, dry clamp.
+// src/timestepper/rungekutta.jl:39-41, src/friction.jl:77,80-84,
+// src/timestepper/timestepper.jl:41-51.
+template <typename T>
+__device__ __forceinline__ void stage1_point(const Phys<T>& p, T tdt, T u0, T u1, T u2, T l0, T l1, T l2, T S, T Bc,
+                                             T& w, T& hu, T& hv) {
+  w = u0 + tdt * l0;
+  hu = u1 + tdt * l1;
+  hv = u2 + tdt * l2;
+  if (p.friction) {
+    const T den = (T)1 - tdt * S;
+    hu = vdiv<T>(hu, den);
+    hv = vdiv<T>(hv, den);
+  }
+  dry_clamp<T>(p, w, hu, hv, Bc);
+}
+
+// ---------------------------------------------------------------------------
+// RK2 stage pass.
+template <typename T>
+struct SmemStage {
+  T U1[3 * HX * HY];
+  T U0[3 * TX * TY];
+  T B[BHX * BHY];
+  T L[3 * LRN];
+  T R[3 * LRN];
+  T F[3 * FN];
+  double dt;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_stage2(Geom<T> g, Phys<T> p, const T* __restrict__ U0, const T* __restrict__ B,
+                                               const T* __restrict__ Lin, const T* __restrict__ Sin, T* __restrict__ Uo,
+                                               StepRecord* rec, int parity) {
+  const bool root = blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0;
+  if (!rec->active[parity]) {
+    if (root) carry_record(rec, parity);
+    return;
+  }
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SmemStage<T>& s = *reinterpret_cast<SmemStage<T>*>(smem_raw);
+  const int tid = threadIdx.x;
+  const int x0 = g.gc + blockIdx.x * TX, y0 = g.gc + blockIdx.y * TY;
+  const int nvx = min(TX, g.gc + g.nx - x0), nvy = min(TY, g.gc + g.ny - y0);
+
+  if (tid == 0) s.dt = step_dt<T>(g, rec, parity);
+  if (!g.bottom_const) load_corners(g, B, s.B, x0, y0);
+  __syncthreads();
+  const double dt = s.dt;
+  const T tdt = (T)dt;
+  BTile<T> bt{s.B, g.bottom_const, g.bconst};
+
+  // U1 on the interior cells of tile + halo, from U0, L, S.
+  for (int idx = tid; idx < HX * HY; idx += NT) {
+    const int lx = idx % HX - 2, ly = idx / HX - 2;
+    const int gx = x0 + lx, gy = y0 + ly;
+    const bool inside = gx >= g.gc && gx < g.gc + g.nx && gy >= g.gc && gy < g.gc + g.ny;
+    T w = (T)0, hu = (T)0, hv = (T)0;
+    if (inside) {
+      const long long o = sidx(g, gx, gy);
+      const T a0 = U0[o], a1 = U0[g.PS + o], a2 = U0[2 * g.PS + o];
+      const T S = p.friction ? Sin[o] : (T)0;
+      stage1_point<T>(p, tdt, a0, a1, a2, Lin[o], Lin[g.PS + o], Lin[2 * g.PS + o], S, bt.cell(lx, ly), w, hu, hv);
+      if (lx >= 0 && lx < TX && ly >= 0 && ly < TY) {
+        const int t = ly * TX + lx;
+        s.U0[t] = a0;
+        s.U0[TX * TY + t] = a1;
+        s.U0[2 * TX * TY + t] = a2;
+      }
+    }
+    s.U1[idx] = w;
+    s.U1[HX * HY + idx] = hu;
+    s.U1[2 * HX * HY + idx] = hv;
+  }
+  __syncthreads();
+  // Wall ghosts of U1 inside the halo (src/bc.jl:81-110); corner ghosts are never read.
+  for (int idx = tid; idx < HX * HY; idx += NT) {
+    const int lx = idx % HX - 2, ly = idx / HX - 2;
+    const int gx = x0 + lx, gy = y0 + ly;
+    const bool xin = gx >= g.gc && gx < g.gc + g.nx;
+    const bool yin = gy >= g.gc && gy < g.gc + g.ny;
+    if (yin && !xin && gx < g.N1) {
+      const int sx = gx < g.gc ? 2 * g.gc - 1 - gx : 2 * (g.gc + g.nx) - 1 - gx;
+      const int si = (ly + 2) * HX + (sx - x0 + 2);
+      s.U1[idx] = s.U1[si];
+      s.U1[HX * HY + idx] = -s.U1[HX * HY + si];
+      s.U1[2 * HX * HY + idx] = s.U1[2 * HX * HY + si];
+    } else if (xin && !yin && gy < g.N2) {
+      const int sy = gy < g.gc ? 2 * g.gc - 1 - gy : 2 * (g.gc + g.ny) - 1 - gy;
+      const int si = (sy - y0 + 2) * HX + (lx + 2);
+      s.U1[idx] = s.U1[si];
+      s.U1[HX * HY + idx] = s.U1[HX * HY + si];
+      s.U1[2 * HX * HY + idx] = -s.U1[2 * HX * HY + si];
+    }
+  }
+  __syncthreads();
+
+  T acc[CPT][3];
+  T mx = (T)0, my = (T)0;
+  tile_derivative<T, false>(p, s.U1, bt, s.L, s.R, s.F, acc, mx, my, nvx, nvy);
+
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    const int c = tid + k * NT;
+    const int lx = c % TX, ly = c / TX;
+    if (lx >= nvx || ly >= nvy) continue;
+    for (int n = 0; n < p.n_point; ++n) acc[k][0] = acc[k][0] + p.point_add[n];
+    const int ci = (ly + 2) * HX + lx + 2;
+    const T v0 = s.U1[ci], v1 = s.U1[HX * HY + ci], v2 = s.U1[2 * HX * HY + ci];
+    T w = v0 + tdt * acc[k][0];
+    T hu = v1 + tdt * acc[k][1];
+    T hv = v2 + tdt * acc[k][2];
+    w = (T)0.5 * (s.U0[c] + w);
+    hu = (T)0.5 * (s.U0[TX * TY + c] + hu);
+    hv = (T)0.5 * (s.U0[2 * TX * TY + c] + hv);
+    const T Bc = bt.cell(lx, ly);
+    if (p.friction) {
+      const T S = friction_factor<T>(p, v0, v1, v2, Bc);
+      const T den = (T)1 - tdt * S;
+      hu = vdiv<T>(hu, den);
+      hv = vdiv<T>(hv, den);
+    }
+    dry_clamp<T>(p, w, hu, hv, Bc);
+    store_with_ghosts<T>(g, Uo, x0 + lx, y0 + ly, w, hu, hv);
+  }
+  if (root) advance_record<T>(rec, parity, dt);
+}
+
+// ---------------------------------------------------------------------------
+// Forward-Euler apply pass: U1 = clamp((U0 + dt*L) ./ (1 .- dt*[0,S,S])).
+template <typename T>
+__global__ void __launch_bounds__(NT) k_apply_fe(Geom<T> g, Phys<T> p, const T* __restrict__ U0,
+                                                 const T* __restrict__ B, const T* __restrict__ Lin,
+                                                 const T* __restrict__ Sin, T* __restrict__ Uo, StepRecord* rec,
+                                                 int parity) {
+  const bool root = blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0;
+  if (!rec->active[parity]) {
+    if (root) carry_record(rec, parity);
+    return;
+  }
+  __shared__ double sdt;
+  if (threadIdx.x == 0) sdt = step_dt<T>(g, rec, parity);
+  __syncthreads();
+  const double dt = sdt;
+  const T tdt = (T)dt;
+  const int lx = threadIdx.x % TX, ly0 = threadIdx.x / TX;
+  for (int ly = ly0; ly < TY; ly += NT / TX) {
+    const int gx = g.gc + blockIdx.x * TX + lx, gy = g.gc + blockIdx.y * TY + ly;
+    if (gx >= g.gc + g.nx || gy >= g.gc + g.ny) continue;
+    const long long o = sidx(g, gx, gy);
+    T Bc = g.bconst;
+    if (!g.bottom_const) {
+      const long long b = (long long)gy * g.PB + gx + XOFF;
+      Bc = (T)0.25 * (((B[b] + B[b + 1]) + B[b + g.PB]) + B[b + g.PB + 1]);
+    }
+    const T S = p.friction ? Sin[o] : (T)0;
+    T w, hu, hv;
+    stage1_point<T>(p, tdt, U0[o], U0[g.PS + o], U0[2 * g.PS + o], Lin[o], Lin[g.PS + o], Lin[2 * g.PS + o], S, Bc, w,
+                    hu, hv);
+    store_with_ghosts<T>(g, Uo, gx, gy, w, hu, hv);
+  }
+  if (root) advance_record<T>(rec, parity, dt);
+}
+
+// Wall boundary update of a whole volume, src/bc.jl:81-110 (used after uploads).
+template <typename T>
+__global__ void k_bc_wall(Geom<T> g, T* __restrict__ U) {
+  const int n_x = g.ny * 2 * g.gc;  // x ghosts at interior rows
+  const int n_y = g.nx * 2 * g.gc;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_x + n_y; idx += gridDim.x * blockDim.x) {
+    if (idx < n_x) {
+      const int j = g.gc + idx / (2 * g.gc), r = idx % (2 * g.gc);
+      const int gx = r < g.gc ? r : g.gc + g.nx + (r - g.gc);
+      const int sx = gx < g.gc ? 2 * g.gc - 1 - gx : 2 * (g.gc + g.nx) - 1 - gx;
+      const long long d = sidx(g, gx, j), sI = sidx(g, sx, j);
+      U[d] = U[sI];
+      U[g.PS + d] = -U[g.PS + sI];
+      U[2 * g.PS + d] = U[2 * g.PS + sI];
+    } else {
+      const int q = idx - n_x;
+      const int i = g.gc + q / (2 * g.gc), r = q % (2 * g.gc);
+      const int gy = r < g.gc ? r : g.gc + g.ny + (r - g.gc);
+      const int sy = gy < g.gc ? 2 * g.gc - 1 - gy : 2 * (g.gc + g.ny) - 1 - gy;
+      const long long d = sidx(g, i, gy), sI = sidx(g, i, sy);
+      U[d] = U[sI];
+      U[g.PS + d] = U[g.PS + sI];
+      U[2 * g.PS + d] = -U[2 * g.PS + sI];
+    }
+  }
+}
+
+// Water volume sum((w - B_cell) * dx * dy) over the interior, in Float64:
+// per-block partial sums in a fixed order, then one block sums the partials.
+template <typename T>
+__global__ void k_volume_partial(Geom<T> g, const T* __restrict__ U, const T* __restrict__ B, double* partial) {
+  __shared__ double red[NT];
+  double acc = 0.0;
+  const long long n = (long long)g.nx * g.ny;
+  for (long long c = (long long)blockIdx.x * NT + threadIdx.x; c < n; c += (long long)gridDim.x * NT) {
+    const int i = g.gc + (int)(c % g.nx), j = g.gc + (int)(c / g.nx);
+    double Bc = (double)g.bconst;
+    if (!g.bottom_const) {
+      const long long b = (long long)j * g.PB + i + XOFF;
+      Bc = (double)((T)0.25 * (((B[b] + B[b + 1]) + B[b + g.PB]) + B[b + g.PB + 1]));
+    }
+    acc += ((double)U[sidx(g, i, j)] - Bc) * g.dx * g.dy;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = NT / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+
+
+}  // namespace vf

@@ -1,0 +1,35 @@
+// vf_launch.cuh -- host-side launchers of the step kernels, one set per real
+// type. The Float64 set lives in vf_f64.cu (built with -fmad=false so every
+// expression rounds as in Julia), the Float32 set in vf_f32.cu.
+#pragma once
+#include "vf_kernels.cuh"
+
+namespace vf {
+
+template <typename T>
+struct StepArgs {
+  Geom<T> g;
+  Phys<T> p;
+  int rk2;
+  const T* B;
+  T* L;
+  T* S;
+  StepRecord* rec;
+};
+
+// One full step reading Uin, writing Uout; parity selects the record slot.
+cudaError_t launch_step(const StepArgs<double>& a, const double* Uin, double* Uout, int parity, cudaStream_t st);
+cudaError_t launch_step(const StepArgs<float>& a, const float* Uin, float* Uout, int parity, cudaStream_t st);
+// Wall boundary update of a whole volume.
+cudaError_t launch_bc(const Geom<double>& g, double* U, cudaStream_t st);
+cudaError_t launch_bc(const Geom<float>& g, float* U, cudaStream_t st);
+// Interior water volume into *out_dev (device double).
+cudaError_t launch_volume(const Geom<double>& g, const double* U, const double* B, double* partial, int nblocks,
+                          double* out_dev, cudaStream_t st);
+cudaError_t launch_volume(const Geom<float>& g, const float* U, const float* B, double* partial, int nblocks,
+                          double* out_dev, cudaStream_t st);
+// Opt the big-shared-memory kernels in on the current device (idempotent).
+cudaError_t configure_kernels_f64();
+cudaError_t configure_kernels_f32();
+
+}  // namespace vf

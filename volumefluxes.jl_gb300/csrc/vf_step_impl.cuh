@@ -1,0 +1,56 @@
+// vf_step_impl.cuh -- launcher bodies shared by the per-precision units.
+#pragma once
+#include "vf_launch.cuh"
+
+namespace vf {
+
+static __global__ void k_volume_final_impl(const double* partial, int n, double* out) {
+  __shared__ double red[NT];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += NT) acc += partial[i];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = NT / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+template <typename T>
+cudaError_t configure_impl() {
+  cudaError_t e = cudaFuncSetAttribute(k_flux<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemFlux<T>));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_stage2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemStage<T>));
+}
+
+template <typename T>
+cudaError_t launch_step_impl(const StepArgs<T>& a, const T* Uin, T* Uout, int parity, cudaStream_t st) {
+  const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + TY - 1) / TY);
+  k_flux<T><<<grid, NT, sizeof(SmemFlux<T>), st>>>(a.g, a.p, Uin, a.B, a.L, a.S, a.rec, parity);
+  if (a.rk2) {
+    k_stage2<T><<<grid, NT, sizeof(SmemStage<T>), st>>>(a.g, a.p, Uin, a.B, a.L, a.S, Uout, a.rec, parity);
+  } else {
+    k_apply_fe<T><<<grid, NT, 0, st>>>(a.g, a.p, Uin, a.B, a.L, a.S, Uout, a.rec, parity);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_bc_impl(const Geom<T>& g, T* U, cudaStream_t st) {
+  const int n = 2 * g.gc * (g.nx + g.ny);
+  int blocks = (n + NT - 1) / NT;
+  if (blocks > 4096) blocks = 4096;
+  k_bc_wall<T><<<blocks, NT, 0, st>>>(g, U);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_volume_impl(const Geom<T>& g, const T* U, const T* B, double* partial, int nblocks, double* out,
+                               cudaStream_t st) {
+  k_volume_partial<T><<<nblocks, NT, 0, st>>>(g, U, B, partial);
+  k_volume_final_impl<<<1, NT, 0, st>>>(partial, nblocks, out);
+  return cudaGetLastError();
+}
+
+}  // namespace vf

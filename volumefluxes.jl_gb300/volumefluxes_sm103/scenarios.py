@@ -1,0 +1,131 @@
+"""Seeded scenario builders for the measured and parity-tested workloads.
+
+  circular_dam_break   2D circular dam break on [0,1]^2, flat bottom, RK2, CFL 0.2
+                       (w = 2 inside radius 0.15 around (0.5, 0.5), else 1).
+  hills_wet_dry        square domain with Δ = 1 m, bottom = sum of seeded Gaussian
+                       hills (amplitude U[0.5,4] m, width U[50,400] m) + 1e-3 * x,
+                       w = max(1.5, B_cell) (dry islands), Manning-type friction
+                       n = 0.03 (friction_bsa2012, Cz = n^2), rain 1e-5 m/s,
+                       infiltration 2e-6 m/s, wall BCs, RK2, CFL 0.25.
+
+Random numbers come from splitmix64 so any language can regenerate them.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import api as vf
+
+MASK64 = (1 << 64) - 1
+
+
+class SplitMix64:
+    """splitmix64 (Steele, Lea & Flood 2014): the state advances by the golden-ratio
+    increment and each output is the state passed through a 64-bit finaliser."""
+
+    def __init__(self, seed: int):
+        self.state = seed & MASK64
+
+    def next_u64(self) -> int:
+        self.state = (self.state + 0x9E3779B97F4A7C15) & MASK64
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & MASK64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & MASK64
+        return z ^ (z >> 31)
+
+    def uniform(self, lo: float = 0.0, hi: float = 1.0) -> float:
+        return lo + (hi - lo) * ((self.next_u64() >> 11) * (1.0 / (1 << 53)))
+
+
+@dataclass
+class Scenario:
+    """Everything needed to build the same run in the library and in the oracle."""
+    name: str
+    nx: int
+    ny: int
+    extent: tuple
+    B: np.ndarray | None            # corners (nx+5, ny+5), None for a flat zero bottom
+    w0: np.ndarray                  # interior (nx, ny)
+    hu0: np.ndarray
+    hv0: np.ndarray
+    cfl: float
+    stepper: str = "rk2"            # "rk2" or "fe"
+    rain_m_per_h: float | None = None
+    infiltration_m_per_s: float | None = None
+    manning_n: float | None = None
+    theta: float = 1.2
+    bottom_source: bool = False
+    friction_law: str = "bsa2012"   # friction_bsa2012 / friction_fcg2016 / friction_bh2021
+    eq: dict = field(default_factory=dict)  # ShallowWaterEquations keywords (rho, g, depth_cutoff, ...)
+    meta: dict = field(default_factory=dict)
+
+    def source_terms(self) -> list:
+        st = []
+        if self.bottom_source:
+            st.append(vf.SourceTermBottom())
+        if self.rain_m_per_h is not None:
+            st.append(vf.ConstantRain(self.rain_m_per_h))
+        if self.infiltration_m_per_s is not None:
+            st.append(vf.ConstantInfiltration(self.infiltration_m_per_s))
+        return st
+
+    def build(self, backend: vf.SM103Backend) -> vf.Simulator:
+        """The scenario script, written against the reference's API."""
+        grid = vf.CartesianGrid(self.nx, self.ny, gc=2, boundary=vf.WallBC(), extent=[list(self.extent[0]),
+                                                                                        list(self.extent[1])])
+        bottom = vf.ConstantBottomTopography() if self.B is None else vf.BottomTopography2D(self.B, backend, grid)
+        eq = vf.ShallowWaterEquations(bottom, **self.eq)
+        friction = None
+        if self.manning_n is not None:
+            law = {"bsa2012": vf.friction_bsa2012, "fcg2016": vf.friction_fcg2016,
+                   "bh2021": vf.friction_bh2021}[self.friction_law]
+            friction = vf.ImplicitFriction(Cz=self.manning_n ** 2, friction_function=law)
+        system = vf.ConservedSystem(backend, vf.LinearReconstruction(self.theta), vf.CentralUpwind(eq), eq, grid,
+                                    self.source_terms(), friction)
+        stepper = vf.RungeKutta2() if self.stepper == "rk2" else vf.ForwardEulerStepper()
+        sim = vf.Simulator(backend, system, stepper, grid, cfl=self.cfl)
+        vf.set_current_state(sim, (self.w0, self.hu0, self.hv0))
+        return sim
+
+
+def circular_dam_break(n: int = 256, radius: float = 0.15, cfl: float = 0.2) -> Scenario:
+    grid = vf.CartesianGrid(n, n, gc=2, boundary=vf.WallBC())
+    c = vf.cell_centers(grid)
+    r = np.sqrt((c[:, :, 0] - 0.5) ** 2 + (c[:, :, 1] - 0.5) ** 2)
+    w0 = np.where(r < radius, 2.0, 1.0)
+    z = np.zeros_like(w0)
+    return Scenario(name=f"circular_dam_break_{n}", nx=n, ny=n, extent=((0.0, 1.0), (0.0, 1.0)), B=None, w0=w0,
+                    hu0=z, hv0=z.copy(), cfl=cfl)
+
+
+def hill_bottom(nx: int, ny: int, extent, n_hills: int, seed: int, slope: float = 1e-3,
+                amp=(0.5, 4.0), width=(50.0, 400.0)) -> np.ndarray:
+    grid = vf.CartesianGrid(nx, ny, gc=2, boundary=vf.WallBC(), extent=[list(extent[0]), list(extent[1])])
+    f = vf.cell_faces(grid, interior=False)
+    x, y = f[:, :, 0], f[:, :, 1]
+    rng = SplitMix64(seed)
+    (x0, x1), (y0, y1) = extent
+    B = slope * x
+    for _ in range(n_hills):
+        cx = rng.uniform(x0, x1)
+        cy = rng.uniform(y0, y1)
+        a = rng.uniform(*amp)
+        s = rng.uniform(*width)
+        B = B + a * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2.0 * s * s))
+    return B
+
+
+def hills_wet_dry(n: int = 4096, seed: int = 20240901, n_hills: int = 64, w_init: float = 1.5,
+                  cfl: float = 0.25, length: float | None = None) -> Scenario:
+    L = float(n) if length is None else float(length)
+    extent = ((0.0, L), (0.0, L))
+    scale = L / 4096.0
+    B = hill_bottom(n, n, extent, n_hills, seed, amp=(0.5, 4.0), width=(50.0 * scale, 400.0 * scale))
+    Bc = 0.25 * (B[:-1, :-1] + B[1:, :-1] + B[:-1, 1:] + B[1:, 1:])[2:-2, 2:-2]
+    w0 = np.maximum(w_init, Bc)
+    z = np.zeros_like(w0)
+    return Scenario(name=f"hills_wet_dry_{n}", nx=n, ny=n, extent=extent, B=B, w0=w0, hu0=z, hv0=z.copy(), cfl=cfl,
+                    rain_m_per_h=1e-5 * 3600, infiltration_m_per_s=2e-6, manning_n=0.03, bottom_source=True,
+                    meta={"seed": seed, "n_hills": n_hills})
