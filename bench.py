@@ -1,0 +1,325 @@
+#!/usr/bin/env python
+"""Throughput of the 2D shallow-water RK2 step (cell-updates/s) on GB300.
+
+Workload: the wet/dry hill terrain at 4096 x 4096 (Δ = 1 m; 64 seeded Gaussian
+hills + 1e-3 slope; w = max(1.5, B_cell); Manning-type friction n = 0.03 via
+friction_bsa2012; rain 1e-5 m/s; infiltration 2e-6 m/s; wall BCs; RK2; CFL
+0.25), Float64 (the parity precision) with the Float32 variant reported
+beside it. One step = one full RK2 step of every interior cell; a
+cell-update = one interior cell advanced by one step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is device throughput with the state resident in HBM (CUDA events on the
+library's stream, max over ranks); `e2e` is the same metric through the public
+API with the state copied from pinned host memory and back every step.
+`--impl reference` times the reference's CPU path (the oracle's restatement of
+it; VolumeFluxes.jl itself is Julia and no Julia toolchain exists on the box)
+on all host cores. Multi-GPU runs are independent replicas (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "volumefluxes.jl_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-updates/s"
+WORDS_PER_CELL_STEP = 17        # stage 1: U0(3)+B(1) in, U1(3) out; stage 2: U1(3)+U0(3)+B(1) in, U2(3) out
+WORDS_STAGE_PASS = 10           # the stage-2 share of those words
+WORDS_FLUX_PASS = 7             # the stage-1 share
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--n", type=int, default=4096)
+    ap.add_argument("--dtype", choices=("f64", "f32"), default="f64")
+    ap.add_argument("--no-variant", action="store_true", help="skip the Float32 variant")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    return ap.parse_args()
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_table():
+    """dram bytes per interior cell per launch, from the committed ncu summaries."""
+    out = {}
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for line in f.read_text().splitlines():
+            if line.startswith("traffic:"):
+                parts = line.split()
+                # traffic: <kernel> <dtype> <bytes_per_cell>
+                if len(parts) == 4:
+                    out[(parts[1], parts[2])] = float(parts[3])
+    return out
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.count(",") >= 8]
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup(backend: str):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, x: float, device=None) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def oracle_sim(sc, real_bytes=8):
+    from oracle import vf_oracle as O
+    src = [(O.SRC_BOTTOM, 0.0), (O.SRC_CONST_RAIN, sc.rain_m_per_h), (O.SRC_CONST_INFIL, sc.infiltration_m_per_s)]
+    o = O.OracleSim(nx=sc.nx, ny=sc.ny, extent=sc.extent, real_bytes=real_bytes, theta=sc.theta, sources=src,
+                    friction=O.FRICTION_BSA2012, friction_Cz=sc.manning_n ** 2, stepper=O.STEPPER_RK2, cfl=sc.cfl,
+                    B=sc.B)
+    o.set_interior(sc.w0, sc.hu0, sc.hv0)
+    return o
+
+
+def cpu_rate(sc, warmup: int, steps: int | None, budget_s: float = 12.0):
+    """Oracle (the restated reference CPU path) on all host threads: cell-updates/s."""
+    from oracle import vf_oracle as O
+    threads = O.set_threads(os.cpu_count() or 1)
+    o = oracle_sim(sc)
+    for _ in range(warmup):
+        o.perform_step(math.inf)
+    if steps is None:
+        t0 = time.perf_counter()
+        o.perform_step(math.inf)
+        one = time.perf_counter() - t0
+        steps = max(1, min(30, int(budget_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.perform_step(math.inf)
+    el = time.perf_counter() - t0
+    return sc.nx * sc.ny * steps / el, threads, steps, el
+
+
+def workload_name(sc, dtype):
+    return (f"hills_wet_dry {sc.nx}x{sc.ny} RK2 {dtype.upper()}: 64 seeded Gaussian hills + 1e-3 slope, "
+            f"w=max(1.5,B), Manning n=0.03 (bsa2012), rain 1e-5 m/s, infiltration 2e-6 m/s, wall BCs, CFL 0.25")
+
+
+def run_reference(args):
+    world, rank, local = dist_setup("gloo")
+    if rank != 0:
+        return
+    from volumefluxes_sm103 import scenarios
+    sc = scenarios.hills_wet_dry(args.n)
+    value, threads, steps, el = cpu_rate(sc, args.warmup, args.steps)
+    sample = f"{steps} full RK2 steps of the {sc.nx}x{sc.ny} Float64 workload after {args.warmup} warm-up steps"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": el / steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(sc, "f64"), "nx": sc.nx, "ny": sc.ny, "parallelism": "replicas"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "VolumeFluxes.jl is Julia and no Julia toolchain exists on the box; the reference arm runs the "
+                "oracle's C++ restatement of its CPU path (same passes, OpenMP over rows)",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def measure_gpu(sc, dtype, args, world, local, lib_time=True):
+    import ctypes as C
+    import volumefluxes_sm103 as vf
+    real = np.float64 if dtype == "f64" else np.float32
+    sim = sc.build(vf.SM103Backend(real, device=local))
+    lib = sim._lib
+    ms = C.c_float()
+    if args.warmup > 0:
+        vf._native.check(lib, sim.handle, lib.vf_time_steps(sim.handle, args.warmup, C.byref(ms)))
+    # headline: K steps back to back, CUDA events on the library's stream
+    barrier(world)
+    n0 = sim.launch_count()
+    with Clocks(local) as clk:
+        vf._native.check(lib, sim.handle, lib.vf_time_steps(sim.handle, args.steps, C.byref(ms)))
+    launches = sim.launch_count() - n0
+    barrier(world)
+    ms_total = allmax(world, float(ms.value))
+    # per-kernel durations (events between the two kernels of every step)
+    mf, mst = C.c_float(), C.c_float()
+    vf._native.check(lib, sim.handle, lib.vf_time_kernels(sim.handle, args.steps, C.byref(mf), C.byref(mst)))
+    return sim, ms_total, mf.value / args.steps, mst.value / args.steps, launches, clk.summary()
+
+
+def e2e_rate(sim, steps: int):
+    """Public API with host buffers: upload state (pinned), one step, download state (pinned)."""
+    import volumefluxes_sm103 as vf
+    g = sim.grid
+    try:
+        import torch
+        bufs = [torch.empty((g.ny, g.nx), dtype=torch.float64 if sim.dtype == np.float64 else torch.float32,
+                            pin_memory=True).numpy() for _ in range(3)]
+    except Exception:
+        bufs = [np.empty((g.ny, g.nx), dtype=sim.dtype) for _ in range(3)]
+    view = vf.StateView(*(b.T for b in bufs))
+    vf.current_interior_state(sim, out=view)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        vf.set_current_state(sim, view)
+        vf.perform_step(sim, math.inf)
+        vf.current_interior_state(sim, out=view)
+    el = time.perf_counter() - t0
+    nbytes = 3 * g.nx * g.ny * sim.dtype.itemsize
+    return g.nx * g.ny * steps / el, nbytes, nbytes, el
+
+
+def roofline(sc, dtype, ms_flux, ms_stage, peak, peak_kind, traffic):
+    e = 8 if dtype == "f64" else 4
+    cells = sc.nx * sc.ny
+    dom_name, dom_ms, words = ("k_stage2", ms_stage, WORDS_STAGE_PASS) if ms_stage >= ms_flux else \
+        ("k_flux", ms_flux, WORDS_FLUX_PASS)
+    alg = words * e * cells
+    ach = alg / (dom_ms * 1e-3) / 1e9
+    tb = traffic.get((dom_name, dtype))
+    return {
+        "bound": "hbm", "kernel": dom_name, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+        "peak_kind": peak_kind, "traffic": (tb * cells) if tb is not None else None,
+        "algorithmic_bytes": alg, "launch_ms": dom_ms,
+    }
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    world, rank, local = dist_setup("nccl")
+    from volumefluxes_sm103 import scenarios
+    sc = scenarios.hills_wet_dry(args.n)
+    peak, peak_kind = peaks()
+    traffic = traffic_table()
+    cells = sc.nx * sc.ny
+    dtypes = [args.dtype] + ([] if args.no_variant else [d for d in ("f64", "f32") if d != args.dtype])
+    results = {}
+    for dt in dtypes:
+        sim, ms_total, ms_flux, ms_stage, launches, clk = measure_gpu(sc, dt, args, world, local)
+        value = world * cells * args.steps / (ms_total * 1e-3)
+        if args.e2e_steps > 0:
+            e2e_v, h2d, d2h, _ = e2e_rate(sim, args.e2e_steps)
+            e2e_v = world * e2e_v  # replicas
+        else:
+            e2e_v, h2d, d2h = None, 0, 0
+        e = 8 if dt == "f64" else 4
+        step_ach = WORDS_PER_CELL_STEP * e * cells / (ms_total / args.steps * 1e-3) / 1e9
+        results[dt] = {
+            "value": value, "ms_per_step": ms_total / args.steps, "gpu_launches": launches, "clocks": clk,
+            "roofline": roofline(sc, dt, ms_flux, ms_stage, peak, peak_kind, traffic),
+            "roofline_step": {"bound": "hbm", "achieved": step_ach, "peak": peak, "unit": "GB/s",
+                              "frac": step_ach / peak, "words_per_cell": WORDS_PER_CELL_STEP},
+            "kernel_ms": {"k_flux": ms_flux, "k_stage2": ms_stage},
+            "e2e": {"value": e2e_v, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        }
+        sim.close()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, threads, steps, el = cpu_rate(sc, 0, None)
+        cpu = {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+               "sample": f"{steps} RK2 steps of the {sc.nx}x{sc.ny} Float64 workload from its initial state "
+                         f"({el:.1f} s, OpenMP over rows)"}
+    if rank != 0:
+        return
+    head = results[args.dtype]
+    line = {
+        "metric": METRIC, "value": head["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
+        "config": {"workload": workload_name(sc, args.dtype), "nx": sc.nx, "ny": sc.ny,
+                   "seed": sc.meta["seed"], "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (state %.0f MB per volume)" % (3 * cells * (8 if args.dtype == 'f64' else 4) / 1e6)},
+        "roofline": head["roofline"], "roofline_step": head["roofline_step"], "kernel_ms": head["kernel_ms"],
+        "cpu_baseline": cpu, "e2e": head["e2e"], "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
+        "variants": {k: v for k, v in results.items() if k != args.dtype},
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

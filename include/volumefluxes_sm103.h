@@ -143,6 +143,11 @@ int vf_stream(vf_handle* h, void** stream);
  * match_endtime = false and max_dt = +Inf, as perform_step!(sim, Inf). */
 int vf_time_steps(vf_handle* h, int64_t n_steps, float* ms_out);
 
+/* Like vf_time_steps, with CUDA events around each kernel of each step:
+ * *ms_flux and *ms_stage receive the summed durations of the flux passes and
+ * of the stage (RK2) or apply (forward Euler) passes. */
+int vf_time_kernels(vf_handle* h, int64_t n_steps, float* ms_flux, float* ms_stage);
+
 /* Message for the last failure on this handle (or of vf_create when h is NULL). */
 const char* vf_last_error(vf_handle* h);
 /* Kernel launches issued by this handle since creation. */

@@ -8,6 +8,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <new>
@@ -100,6 +101,9 @@ void fill_phys(const vf_handle* h, vf::Phys<T>& p) {
   p.inv_dy = (T)(1 / dy);
   p.dx = (T)dx;
   p.dy = (T)dy;
+  int ex = 0;
+  p.dx_pow2 = std::frexp(dx, &ex) == 0.5 ? 1 : 0;
+  p.dy_pow2 = std::frexp(dy, &ex) == 0.5 ? 1 : 0;
   p.Cz = (T)c.friction_Cz;
   p.friction = c.friction;
   p.n_bottom = 0;
@@ -299,6 +303,9 @@ int vf_create(const vf_config* cfg, vf_handle** out) {
   fill_geom(h, h->af.g);
   fill_phys(h, h->af.p);
   h->ad.rk2 = h->af.rk2 = cfg->stepper == VF_STEPPER_RK2;
+  // VF_KERNELS=tile selects the shared-memory tile kernels (kept for comparison).
+  const char* kv = std::getenv("VF_KERNELS");
+  h->ad.variant = h->af.variant = (kv && std::strcmp(kv, "tile") == 0) ? 1 : 0;
   h->ad.B = static_cast<const double*>(h->B);
   h->ad.L = static_cast<double*>(h->L);
   h->ad.S = static_cast<double*>(h->S);
@@ -459,6 +466,56 @@ int vf_time_steps(vf_handle* h, int64_t n_steps, float* ms_out) {
   if ((rc = pull_record(h))) return rc;
   if (h->rec_h->n_done & 1) std::swap(h->U[0], h->U[1]);
   if (ms_out) *ms_out = ms;
+  return VF_OK;
+}
+
+int vf_time_kernels(vf_handle* h, int64_t n_steps, float* ms_flux, float* ms_stage) {
+  int rc = ensure_ready(h);
+  if (rc) return rc;
+  if (n_steps < 1) return fail(h, VF_EINVAL, "n_steps must be >= 1");
+  reset_record(h);
+  h->rec_h->active[0] = 1;
+  if ((rc = push_record(h))) return rc;
+  const long long ne = 2 * n_steps + 1;
+  cudaEvent_t* ev = new (std::nothrow) cudaEvent_t[ne];
+  if (!ev) return fail(h, VF_ENOMEM, "host allocation failed");
+  for (long long i = 0; i < ne; ++i) VF_CK(h, cudaEventCreate(&ev[i]));
+  VF_CK(h, cudaEventRecord(ev[0], h->stream));
+  for (long long k = 0; k < n_steps; ++k) {
+    const int parity = (int)(k & 1);
+    cudaError_t e;
+    if (h->elem == 8) {
+      e = vf::launch_flux(h->ad, static_cast<const double*>(h->U[parity]), parity, h->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[2 * k + 1], h->stream);
+      if (e == cudaSuccess)
+        e = vf::launch_stage(h->ad, static_cast<const double*>(h->U[parity]), static_cast<double*>(h->U[parity ^ 1]),
+                             parity, h->stream);
+    } else {
+      e = vf::launch_flux(h->af, static_cast<const float*>(h->U[parity]), parity, h->stream);
+      if (e == cudaSuccess) e = cudaEventRecord(ev[2 * k + 1], h->stream);
+      if (e == cudaSuccess)
+        e = vf::launch_stage(h->af, static_cast<const float*>(h->U[parity]), static_cast<float*>(h->U[parity ^ 1]),
+                             parity, h->stream);
+    }
+    h->launches += 2;
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2 * k + 2], h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "timed step");
+  }
+  VF_CK(h, cudaEventSynchronize(ev[ne - 1]));
+  float f = 0.f, s = 0.f;
+  for (long long k = 0; k < n_steps; ++k) {
+    float a = 0.f, b = 0.f;
+    VF_CK(h, cudaEventElapsedTime(&a, ev[2 * k], ev[2 * k + 1]));
+    VF_CK(h, cudaEventElapsedTime(&b, ev[2 * k + 1], ev[2 * k + 2]));
+    f += a;
+    s += b;
+  }
+  for (long long i = 0; i < ne; ++i) cudaEventDestroy(ev[i]);
+  delete[] ev;
+  if ((rc = pull_record(h))) return rc;
+  if (h->rec_h->n_done & 1) std::swap(h->U[0], h->U[1]);
+  if (ms_flux) *ms_flux = f;
+  if (ms_stage) *ms_stage = s;
   return VF_OK;
 }
 

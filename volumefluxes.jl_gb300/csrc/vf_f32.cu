@@ -6,6 +6,12 @@ namespace vf {
 cudaError_t launch_step(const StepArgs<float>& a, const float* Uin, float* Uout, int parity, cudaStream_t st) {
   return launch_step_impl<float>(a, Uin, Uout, parity, st);
 }
+cudaError_t launch_flux(const StepArgs<float>& a, const float* Uin, int parity, cudaStream_t st) {
+  return launch_flux_impl<float>(a, Uin, parity, st);
+}
+cudaError_t launch_stage(const StepArgs<float>& a, const float* Uin, float* Uout, int parity, cudaStream_t st) {
+  return launch_stage_impl<float>(a, Uin, Uout, parity, st);
+}
 cudaError_t launch_bc(const Geom<float>& g, float* U, cudaStream_t st) { return launch_bc_impl<float>(g, U, st); }
 cudaError_t launch_volume(const Geom<float>& g, const float* U, const float* B, double* partial, int nblocks,
                           double* out, cudaStream_t st) {

@@ -7,6 +7,12 @@ namespace vf {
 cudaError_t launch_step(const StepArgs<double>& a, const double* Uin, double* Uout, int parity, cudaStream_t st) {
   return launch_step_impl<double>(a, Uin, Uout, parity, st);
 }
+cudaError_t launch_flux(const StepArgs<double>& a, const double* Uin, int parity, cudaStream_t st) {
+  return launch_flux_impl<double>(a, Uin, parity, st);
+}
+cudaError_t launch_stage(const StepArgs<double>& a, const double* Uin, double* Uout, int parity, cudaStream_t st) {
+  return launch_stage_impl<double>(a, Uin, Uout, parity, st);
+}
 cudaError_t launch_bc(const Geom<double>& g, double* U, cudaStream_t st) { return launch_bc_impl<double>(g, U, st); }
 cudaError_t launch_volume(const Geom<double>& g, const double* U, const double* B, double* partial, int nblocks,
                           double* out, cudaStream_t st) {

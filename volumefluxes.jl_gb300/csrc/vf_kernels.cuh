@@ -154,7 +154,7 @@ __device__ __forceinline__ void tile_derivative(const Phys<T>& p, const T* sU, c
     const int rc = ly * (TX + 2) + lx + 1;
     for (int b = 0; b < p.n_bottom; ++b) {
       const T Bl = bt.template face_l<0>(lx, ly), Br = bt.template face_r<0>(lx, ly);
-      acc[k][1] = acc[k][1] + p.neg_g * vdiv<T>(Br - Bl, p.dx) * ((sR[rc] + sL[rc]) * (T)0.5);
+      acc[k][1] = acc[k][1] + p.neg_g * slope_over<T>(Br - Bl, p.dx, p.inv_dx, p.dx_pow2) * ((sR[rc] + sL[rc]) * (T)0.5);
     }
   }
   __syncthreads();
@@ -201,7 +201,7 @@ __device__ __forceinline__ void tile_derivative(const Phys<T>& p, const T* sU, c
     const int rc = (ly + 1) * TX + lx;
     for (int b = 0; b < p.n_bottom; ++b) {
       const T Bl = bt.template face_l<1>(lx, ly), Br = bt.template face_r<1>(lx, ly);
-      acc[k][2] = acc[k][2] + p.neg_g * vdiv<T>(Br - Bl, p.dy) * ((sR[rc] + sL[rc]) * (T)0.5);
+      acc[k][2] = acc[k][2] + p.neg_g * slope_over<T>(Br - Bl, p.dy, p.inv_dy, p.dy_pow2) * ((sR[rc] + sL[rc]) * (T)0.5);
     }
   }
 }
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(NT) k_flux(Geom<T> g, Phys<T> p, const T* __re
     const int c = tid + k * NT;
     const int lx = c % TX, ly = c / TX;
     if (lx >= nvx || ly >= nvy) continue;
-    for (int n = 0; n < p.n_point; ++n) acc[k][0] = acc[k][0] + p.point_add[n];
+    acc[k][0] = add_point_sources<T>(p, acc[k][0]);
     const long long o = sidx(g, x0 + lx, y0 + ly);
 #pragma unroll
     for (int j = 0; j < 3; ++j) Lout[j * g.PS + o] = acc[k][j];
@@ -385,11 +385,7 @@ __device__ __forceinline__ void stage1_point(const Phys<T>& p, T tdt, T u0, T u1
   w = u0 + tdt * l0;
   hu = u1 + tdt * l1;
   hv = u2 + tdt * l2;
-  if (p.friction) {
-    const T den = (T)1 - tdt * S;
-    hu = vdiv<T>(hu, den);
-    hv = vdiv<T>(hv, den);
-  }
+  if (p.friction) apply_friction<T>(tdt, S, hu, hv);
   dry_clamp<T>(p, w, hu, hv, Bc);
 }
 
@@ -482,7 +478,7 @@ __global__ void __launch_bounds__(NT) k_stage2(Geom<T> g, Phys<T> p, const T* __
     const int c = tid + k * NT;
     const int lx = c % TX, ly = c / TX;
     if (lx >= nvx || ly >= nvy) continue;
-    for (int n = 0; n < p.n_point; ++n) acc[k][0] = acc[k][0] + p.point_add[n];
+    acc[k][0] = add_point_sources<T>(p, acc[k][0]);
     const int ci = (ly + 2) * HX + lx + 2;
     const T v0 = s.U1[ci], v1 = s.U1[HX * HY + ci], v2 = s.U1[2 * HX * HY + ci];
     T w = v0 + tdt * acc[k][0];

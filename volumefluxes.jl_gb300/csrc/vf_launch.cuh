@@ -2,7 +2,7 @@
 // type. The Float64 set lives in vf_f64.cu (built with -fmad=false so every
 // expression rounds as in Julia), the Float32 set in vf_f32.cu.
 #pragma once
-#include "vf_kernels.cuh"
+#include "vf_march.cuh"
 
 namespace vf {
 
@@ -11,6 +11,7 @@ struct StepArgs {
   Geom<T> g;
   Phys<T> p;
   int rk2;
+  int variant;  // 0: column-marching kernels, 1: shared-memory tile kernels
   const T* B;
   T* L;
   T* S;
@@ -20,6 +21,11 @@ struct StepArgs {
 // One full step reading Uin, writing Uout; parity selects the record slot.
 cudaError_t launch_step(const StepArgs<double>& a, const double* Uin, double* Uout, int parity, cudaStream_t st);
 cudaError_t launch_step(const StepArgs<float>& a, const float* Uin, float* Uout, int parity, cudaStream_t st);
+// The two kernels of a step, separately (for per-kernel timing).
+cudaError_t launch_flux(const StepArgs<double>& a, const double* Uin, int parity, cudaStream_t st);
+cudaError_t launch_flux(const StepArgs<float>& a, const float* Uin, int parity, cudaStream_t st);
+cudaError_t launch_stage(const StepArgs<double>& a, const double* Uin, double* Uout, int parity, cudaStream_t st);
+cudaError_t launch_stage(const StepArgs<float>& a, const float* Uin, float* Uout, int parity, cudaStream_t st);
 // Wall boundary update of a whole volume.
 cudaError_t launch_bc(const Geom<double>& g, double* U, cudaStream_t st);
 cudaError_t launch_bc(const Geom<float>& g, float* U, cudaStream_t st);

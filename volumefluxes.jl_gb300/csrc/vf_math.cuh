@@ -4,8 +4,12 @@
 // Every expression keeps the reference's operation order, because the Float64
 // path must reproduce the reference bit for bit: the Float64 translation unit
 // is compiled with -fmad=false, so a*b+c stays two rounded operations as in
-// Julia. Float32 instances may contract (their error is stated against the
-// Float64 oracle, not claimed bitwise).
+// Julia. Float32 instances may contract and use fast reciprocals (their error
+// is stated against the Float64 oracle, not claimed bitwise).
+//
+// GB300 executes Float64 at 1/64 of the Float32 rate, so the Float64 traits
+// below move every comparison, min/max and sign test onto the integer pipe by
+// comparing IEEE bit patterns; only +, -, *, /, sqrt stay on the FP64 pipe.
 //
 // Citations are path:line within the VolumeFluxes.jl project.
 #pragma once
@@ -14,24 +18,60 @@
 
 namespace vf {
 
-// Julia's min/max on IEEE floats order -0.0 below +0.0
-// (relevant when a dry face contributes +0 against a -0 eigenvalue).
-// NaN operands cannot occur on a valid step (every divisor is bounded away
-// from zero), so NaN ordering is not reproduced here.
+// ---------------------------------------------------------------------------
+// Precision traits.
 template <typename T>
-__device__ __forceinline__ T jmax(T x, T y) {
-  return (x > y || (x == y && !signbit(x))) ? x : y;
-}
-template <typename T>
-__device__ __forceinline__ T jmin(T x, T y) {
-  return (x < y || (x == y && signbit(x))) ? x : y;
-}
+struct Arith;
 
-// Division. Float64 keeps IEEE division (bitwise parity); Float32 may use the
-// fast reciprocal path.
-template <typename T> __device__ __forceinline__ T vdiv(T a, T b);
-template <> __device__ __forceinline__ double vdiv<double>(double a, double b) { return a / b; }
-template <> __device__ __forceinline__ float vdiv<float>(float a, float b) { return __fdividef(a, b); }
+// Float64: exact IEEE semantics. Comparisons are done on bit patterns (valid
+// for every non-NaN operand; a valid step never produces NaN because every
+// divisor is bounded away from zero).
+template <>
+struct Arith<double> {
+  static constexpr bool exact = true;
+  static __device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
+  // Monotone key: orders all non-NaN doubles, with -0.0 just below +0.0.
+  static __device__ __forceinline__ long long key(double x) {
+    const long long b = bits(x);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+  }
+  static __device__ __forceinline__ bool both_zero(double x, double y) {
+    return ((unsigned long long)(bits(x) | bits(y)) << 1) == 0ull;
+  }
+  static __device__ __forceinline__ bool lt(double x, double y) { return key(x) < key(y) && !both_zero(x, y); }
+  static __device__ __forceinline__ bool gt(double x, double y) { return key(x) > key(y) && !both_zero(x, y); }
+  static __device__ __forceinline__ bool gt0(double x) { return bits(x) > 0; }
+  static __device__ __forceinline__ bool lt0(double x) {
+    return (unsigned long long)bits(x) > 0x8000000000000000ull;
+  }
+  // |x| < k and |x| >= k for k >= 0.
+  static __device__ __forceinline__ bool abs_lt(double x, double k) {
+    return (unsigned long long)(bits(x) & 0x7fffffffffffffffll) < (unsigned long long)bits(k);
+  }
+  static __device__ __forceinline__ bool is_zero(double x) { return (bits(x) << 1) == 0ll; }
+  // Julia's max/min: -0.0 < +0.0.
+  static __device__ __forceinline__ double max(double x, double y) { return key(x) > key(y) ? x : y; }
+  static __device__ __forceinline__ double min(double x, double y) { return key(x) < key(y) ? x : y; }
+  static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+  static __device__ __forceinline__ double rcp(double b) { return 1.0 / b; }
+  static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+};
+
+template <>
+struct Arith<float> {
+  static constexpr bool exact = false;
+  static __device__ __forceinline__ bool lt(float x, float y) { return x < y; }
+  static __device__ __forceinline__ bool gt(float x, float y) { return x > y; }
+  static __device__ __forceinline__ bool gt0(float x) { return x > 0.f; }
+  static __device__ __forceinline__ bool lt0(float x) { return x < 0.f; }
+  static __device__ __forceinline__ bool abs_lt(float x, float k) { return fabsf(x) < k; }
+  static __device__ __forceinline__ bool is_zero(float x) { return x == 0.f; }
+  static __device__ __forceinline__ float max(float x, float y) { return fmaxf(x, y); }
+  static __device__ __forceinline__ float min(float x, float y) { return fminf(x, y); }
+  static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+  static __device__ __forceinline__ float rcp(float b) { return __frcp_rn(b); }
+  static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+};
 
 // ---------------------------------------------------------------------------
 // Correctly rounded cube root (Float64). A libm seed is corrected with an exact
@@ -103,6 +143,11 @@ template <typename T> __device__ __forceinline__ T vcbrt(T x);
 template <> __device__ __forceinline__ double vcbrt<double>(double x) { return cr_cbrt(x); }
 template <> __device__ __forceinline__ float vcbrt<float>(float x) { return cbrtf(x); }
 
+// Back-compat names used by the tile kernels.
+template <typename T> __device__ __forceinline__ T jmax(T x, T y) { return Arith<T>::max(x, y); }
+template <typename T> __device__ __forceinline__ T jmin(T x, T y) { return Arith<T>::min(x, y); }
+template <typename T> __device__ __forceinline__ T vdiv(T a, T b) { return Arith<T>::div(a, b); }
+
 // ---------------------------------------------------------------------------
 // Physical constants of one simulation in the state's real type.
 template <typename T>
@@ -111,6 +156,7 @@ struct Phys {
   T cutoff, kappa, theta;
   T inv_dx, inv_dy;           // 1/Δx, 1/Δy (src/numericalflux/numericalflux.jl:27)
   T dx, dy;                   // Δx, Δy (src/sourceterms/source_term_bottom.jl:38)
+  int dx_pow2, dy_pow2;       // Δ is a power of two: x/Δ == x*(1/Δ) exactly
   T Cz;
   int friction;               // VF_FRICTION_*
   int n_bottom;               // SourceTermBottom entries
@@ -118,23 +164,47 @@ struct Phys {
   T point_add[8];             // +rate/3600 for rain, -rate for infiltration
 };
 
+// ΔB/Δ of the bottom source; exact reciprocal multiply when Δ is a power of two.
+template <typename T>
+__device__ __forceinline__ T slope_over(T dB, T delta, T inv_delta, int pow2) {
+  return pow2 ? dB * inv_delta : Arith<T>::div(dB, delta);
+}
+
+// Rain and infiltration in list order (src/system.jl:71-73), unrolled so the
+// parameter block is never indexed dynamically.
+template <typename T>
+__device__ __forceinline__ T add_point_sources(const Phys<T>& p, T acc0) {
+#pragma unroll
+  for (int n = 0; n < 8; ++n)
+    if (n < p.n_point) acc0 = acc0 + p.point_add[n];
+  return acc0;
+}
+
 // desingularize, src/equations/equation.jl:40-62 (Eq. 26 of Brodtkorb & Holm 2021).
 // For |h| >= kappa the expression equals h exactly: min(...) <= kappa <= |h|.
 template <typename T>
 __device__ __forceinline__ T desing(T h, T kappa) {
-  const T ah = fabs(h);
-  if (ah >= kappa) return h;
-  const T m = jmin<T>(vdiv<T>(h * h, (T)2 * kappa) + kappa / (T)2, kappa);
-  return copysign((T)1, h) * jmax<T>(ah, m);
+  using A = Arith<T>;
+  if (!A::abs_lt(h, kappa)) return h;
+  const T m = A::min(A::div(h * h, (T)2 * kappa) + kappa / (T)2, kappa);
+  return copysign((T)1, h) * A::max(fabs(h), m);
 }
 
 // One side of a face: physical flux (src/equations/swe_2D.jl:43-65) and the
 // two outer eigenvalues (src/equations/swe_2D.jl:69-81).
 template <typename T, int DIR>
 __device__ __forceinline__ void side_flux(const Phys<T>& p, T h, T hu, T hv, T& f0, T& f1, T& f2, T& l1, T& l2) {
+  using A = Arith<T>;
   const T hs = desing<T>(h, p.kappa);
-  const T u = vdiv<T>(hu, hs);
-  const T v = vdiv<T>(hv, hs);
+  T u, v;
+  if (A::exact) {
+    u = A::div(hu, hs);
+    v = A::div(hv, hs);
+  } else {
+    const T r = A::rcp(hs);
+    u = hu * r;
+    v = hv * r;
+  }
   const T rh = p.rho * h;
   const T hh = h * h;
   if (DIR == 0) {
@@ -146,7 +216,7 @@ __device__ __forceinline__ void side_flux(const Phys<T>& p, T h, T hu, T hv, T& 
     f1 = (rh * u) * v;
     f2 = f0 * v + p.c2 * hh;
   }
-  const T c = sqrt(p.g * h);
+  const T c = A::sqrt_(p.g * h);
   const T un = DIR == 0 ? u : v;
   l1 = un + c;
   l2 = un - c;
@@ -157,30 +227,41 @@ __device__ __forceinline__ void side_flux(const Phys<T>& p, T h, T hu, T hv, T& 
 template <typename T, int DIR, bool SPEED>
 __device__ __forceinline__ void cu_face(const Phys<T>& p, T mh, T mhu, T mhv, T ph, T phu, T phv, T& F0, T& F1, T& F2,
                                         T& speed) {
+  using A = Arith<T>;
   T fm0 = 0, fm1 = 0, fm2 = 0, em1 = 0, em2 = 0;
-  if (mh > p.cutoff) side_flux<T, DIR>(p, mh, mhu, mhv, fm0, fm1, fm2, em1, em2);
+  if (A::gt(mh, p.cutoff)) side_flux<T, DIR>(p, mh, mhu, mhv, fm0, fm1, fm2, em1, em2);
   T fp0 = 0, fp1 = 0, fp2 = 0, ep1 = 0, ep2 = 0;
-  if (ph > p.cutoff) side_flux<T, DIR>(p, ph, phu, phv, fp0, fp1, fp2, ep1, ep2);
-  const T aplus = jmax<T>(jmax<T>(ep1, em1), (T)0);
-  const T aminus = jmin<T>(jmin<T>(ep2, em2), (T)0);
+  if (A::gt(ph, p.cutoff)) side_flux<T, DIR>(p, ph, phu, phv, fp0, fp1, fp2, ep1, ep2);
+  const T aplus = A::max(A::max(ep1, em1), (T)0);
+  const T aminus = A::min(A::min(ep2, em2), (T)0);
   const T d = aplus - aminus;
-  if (fabs(d) < p.kappa) {
+  if (A::abs_lt(d, p.kappa)) {
     F0 = F1 = F2 = (T)0;
     if (SPEED) speed = (T)0;
     return;
   }
-  const T q = vdiv<T>(aplus * aminus, d);
-  F0 = vdiv<T>(aplus * fm0 - aminus * fp0, d) + q * (ph - mh);
-  F1 = vdiv<T>(aplus * fm1 - aminus * fp1, d) + q * (phu - mhu);
-  F2 = vdiv<T>(aplus * fm2 - aminus * fp2, d) + q * (phv - mhv);
-  if (SPEED) speed = (mh < p.cutoff && ph < p.cutoff) ? (T)0 : jmax<T>(fabs(aplus), fabs(aminus));
+  if (A::exact) {
+    const T q = A::div(aplus * aminus, d);
+    F0 = A::div(aplus * fm0 - aminus * fp0, d) + q * (ph - mh);
+    F1 = A::div(aplus * fm1 - aminus * fp1, d) + q * (phu - mhu);
+    F2 = A::div(aplus * fm2 - aminus * fp2, d) + q * (phv - mhv);
+  } else {
+    const T r = A::rcp(d);
+    const T q = aplus * aminus * r;
+    F0 = (aplus * fm0 - aminus * fp0) * r + q * (ph - mh);
+    F1 = (aplus * fm1 - aminus * fp1) * r + q * (phu - mhu);
+    F2 = (aplus * fm2 - aminus * fp2) * r + q * (phv - mhv);
+  }
+  if (SPEED)
+    speed = (A::lt(mh, p.cutoff) && A::lt(ph, p.cutoff)) ? (T)0 : A::max(fabs(aplus), fabs(aminus));
 }
 
 // minmod and minmod_slope, src/reconstruction/linearreconstruction.jl:28-43.
 template <typename T>
 __device__ __forceinline__ T minmod(T a, T b, T c) {
-  if (a > (T)0 && b > (T)0 && c > (T)0) return jmin<T>(jmin<T>(a, b), c);
-  if (a < (T)0 && b < (T)0 && c < (T)0) return jmax<T>(jmax<T>(a, b), c);
+  using A = Arith<T>;
+  if (A::gt0(a) && A::gt0(b) && A::gt0(c)) return A::min(A::min(a, b), c);
+  if (A::lt0(a) && A::lt0(b) && A::lt0(c)) return A::max(A::max(a, b), c);
   return (T)0;
 }
 template <typename T>
@@ -197,13 +278,14 @@ __device__ __forceinline__ T minmod_slope(T l, T c, T r, T theta) {
 template <typename T>
 __device__ __forceinline__ void reconstruct_cell(const Phys<T>& p, const T l[3], const T c[3], const T r[3], T Bl, T Br,
                                                  T L[3], T R[3]) {
+  using A = Arith<T>;
   T s0 = minmod_slope<T>(l[0], c[0], r[0], p.theta);
   const T s1 = minmod_slope<T>(l[1], c[1], r[1], p.theta);
   const T s2 = minmod_slope<T>(l[2], c[2], r[2], p.theta);
   const T w = c[0];
-  if (w - (T)0.5 * s0 < Bl) {
+  if (A::lt(w - (T)0.5 * s0, Bl)) {
     s0 = (T)2 * (w - Bl);
-  } else if (w + (T)0.5 * s0 < Br) {
+  } else if (A::lt(w + (T)0.5 * s0, Br)) {
     s0 = (T)2 * (Br - w);
   }
   L[0] = (c[0] - (T)0.5 * s0) - Bl;
@@ -216,12 +298,26 @@ __device__ __forceinline__ void reconstruct_cell(const Phys<T>& p, const T l[3],
 
 // Friction factor of ImplicitFriction for a 2D cell, src/friction.jl:30-43,62-78:
 // S = law(Cz, h*, |u|) with h* = desingularize(w - B_cell) and u = (hu, hv)/h*.
+// When hu and hv are both zero, S is -0 and the implicit division is by 1:
+// callers may skip it (friction_active).
+template <typename T>
+__device__ __forceinline__ bool friction_active(T hu, T hv) {
+  return !(Arith<T>::is_zero(hu) && Arith<T>::is_zero(hv));
+}
 template <typename T>
 __device__ __forceinline__ T friction_factor(const Phys<T>& p, T w, T hu, T hv, T Bc) {
+  using A = Arith<T>;
   const T hs = desing<T>(w - Bc, p.kappa);
-  const T u = vdiv<T>(hu, hs);
-  const T v = vdiv<T>(hv, hs);
-  const T speed = sqrt(u * u + v * v);
+  T u, v;
+  if (A::exact) {
+    u = A::div(hu, hs);
+    v = A::div(hv, hs);
+  } else {
+    const T r = A::rcp(hs);
+    u = hu * r;
+    v = hv * r;
+  }
+  const T speed = A::sqrt_(u * u + v * v);
   T denom;
   if (p.friction == 1) {          // friction_bsa2012
     denom = vcbrt<T>(hs) * hs;
@@ -230,14 +326,32 @@ __device__ __forceinline__ T friction_factor(const Phys<T>& p, T w, T hu, T hv, 
   } else {                        // friction_bh2021
     denom = hs * hs;
   }
-  return vdiv<T>(-p.Cz * speed, denom);
+  return A::div(-p.Cz * speed, denom);
+}
+
+// out[1:2] ./= (1 - dt*S) (src/friction.jl:77); skipped when S is zero, where
+// the division is by exactly 1.
+template <typename T>
+__device__ __forceinline__ void apply_friction(T tdt, T S, T& hu, T& hv) {
+  using A = Arith<T>;
+  if (A::is_zero(S)) return;
+  const T den = (T)1 - tdt * S;
+  if (A::exact) {
+    hu = A::div(hu, den);
+    hv = A::div(hv, den);
+  } else {
+    const T r = A::rcp(den);
+    hu = hu * r;
+    hv = hv * r;
+  }
 }
 
 // Dry-cell clamp, src/timestepper/timestepper.jl:41-51.
 template <typename T>
 __device__ __forceinline__ void dry_clamp(const Phys<T>& p, T& w, T& hu, T& hv, T Bc) {
-  if (w - Bc < p.cutoff) {
-    w = jmax<T>(w, Bc);
+  using A = Arith<T>;
+  if (A::lt(w - Bc, p.cutoff)) {
+    w = A::max(w, Bc);
     hu = (T)0;
     hv = (T)0;
   }

@@ -17,6 +17,9 @@ static __global__ void k_volume_final_impl(const double* partial, int n, double*
   if (threadIdx.x == 0) *out = red[0];
 }
 
+// Rows per marching segment.
+template <typename T> struct MarchSeg { static constexpr int value = 64; };
+
 template <typename T>
 cudaError_t configure_impl() {
   cudaError_t e = cudaFuncSetAttribute(k_flux<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemFlux<T>));
@@ -25,15 +28,42 @@ cudaError_t configure_impl() {
 }
 
 template <typename T>
-cudaError_t launch_step_impl(const StepArgs<T>& a, const T* Uin, T* Uout, int parity, cudaStream_t st) {
+dim3 march_grid(const Geom<T>& g) {
+  const int nstrips = (g.nx + MOUT - 1) / MOUT;
+  return dim3((nstrips + MWPB - 1) / MWPB, (g.ny + MarchSeg<T>::value - 1) / MarchSeg<T>::value);
+}
+
+template <typename T>
+cudaError_t launch_flux_impl(const StepArgs<T>& a, const T* Uin, int parity, cudaStream_t st) {
+  if (a.variant == 0) {
+    k_flux_march<T, MarchSeg<T>::value><<<march_grid(a.g), MW * MWPB, 0, st>>>(a.g, a.p, Uin, a.B, a.L, a.S, a.rec,
+                                                                                parity);
+    return cudaGetLastError();
+  }
   const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + TY - 1) / TY);
   k_flux<T><<<grid, NT, sizeof(SmemFlux<T>), st>>>(a.g, a.p, Uin, a.B, a.L, a.S, a.rec, parity);
-  if (a.rk2) {
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_stage_impl(const StepArgs<T>& a, const T* Uin, T* Uout, int parity, cudaStream_t st) {
+  const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + TY - 1) / TY);
+  if (a.rk2 && a.variant == 0) {
+    k_stage_march<T, MarchSeg<T>::value><<<march_grid(a.g), MW * MWPB, 0, st>>>(a.g, a.p, Uin, a.B, a.L, a.S, Uout,
+                                                                                 a.rec, parity);
+  } else if (a.rk2) {
     k_stage2<T><<<grid, NT, sizeof(SmemStage<T>), st>>>(a.g, a.p, Uin, a.B, a.L, a.S, Uout, a.rec, parity);
   } else {
     k_apply_fe<T><<<grid, NT, 0, st>>>(a.g, a.p, Uin, a.B, a.L, a.S, Uout, a.rec, parity);
   }
   return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_step_impl(const StepArgs<T>& a, const T* Uin, T* Uout, int parity, cudaStream_t st) {
+  cudaError_t e = launch_flux_impl<T>(a, Uin, parity, st);
+  if (e != cudaSuccess) return e;
+  return launch_stage_impl<T>(a, Uin, Uout, parity, st);
 }
 
 template <typename T>

@@ -26,7 +26,7 @@ VF_REC_LINEAR = 1
 EXPORTED_SYMBOLS = (
     "vf_create", "vf_destroy", "vf_upload_bottom", "vf_set_interior_state", "vf_upload_state",
     "vf_download_state", "vf_get_interior_state", "vf_step", "vf_simulate", "vf_water_volume",
-    "vf_device_state", "vf_stream", "vf_time_steps", "vf_last_error", "vf_launch_count",
+    "vf_device_state", "vf_stream", "vf_time_steps", "vf_time_kernels", "vf_last_error", "vf_launch_count",
 )
 
 
@@ -96,6 +96,7 @@ def load(build_if_missing: bool = False):
                                       C.POINTER(C.c_int64)]),
         "vf_stream": (C.c_int, [H, C.POINTER(C.c_void_p)]),
         "vf_time_steps": (C.c_int, [H, C.c_int64, C.POINTER(C.c_float)]),
+        "vf_time_kernels": (C.c_int, [H, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "vf_last_error": (C.c_char_p, [H]),
         "vf_launch_count": (C.c_int64, [H]),
     }

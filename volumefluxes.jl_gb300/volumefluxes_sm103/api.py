@@ -583,13 +583,25 @@ def set_current_state(simulator: Simulator, new_state) -> None:
     N.check(lib, simulator.handle, lib.vf_set_interior_state(simulator.handle, N.ptr(w), N.ptr(hu), N.ptr(hv)))
 
 
-def current_interior_state(simulator: Simulator) -> StateView:
-    """collect(current_interior_state(simulator).h/.hu/.hv), src/simulator.jl:114-115."""
+def current_interior_state(simulator: Simulator, out: StateView | None = None) -> StateView:
+    """collect(current_interior_state(simulator).h/.hu/.hv), src/simulator.jl:114-115.
+
+    With `out`, the planes are written into its (nx, ny) arrays, which must be
+    x-fastest (the transpose of a C-contiguous (ny, nx) array) of the backend's
+    real type -- e.g. views of pinned host buffers."""
     g = simulator.grid
-    planes = [np.empty((g.ny, g.nx), dtype=simulator.dtype) for _ in range(3)]
+    if out is None:
+        planes = [np.empty((g.ny, g.nx), dtype=simulator.dtype) for _ in range(3)]
+        result = StateView(*(p.T for p in planes))
+    else:
+        planes = [a.T for a in (out.h, out.hu, out.hv)]
+        for p in planes:
+            if p.shape != (g.ny, g.nx) or p.dtype != simulator.dtype or not p.flags.c_contiguous:
+                raise ArgumentError("out planes must be x-fastest (nx, ny) arrays of the backend's real type")
+        result = out
     lib = simulator._lib
     N.check(lib, simulator.handle, lib.vf_get_interior_state(simulator.handle, *(N.ptr(p) for p in planes)))
-    return StateView(*(p.T for p in planes))
+    return result
 
 
 def current_state(simulator: Simulator) -> StateView:
