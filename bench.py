@@ -45,7 +45,7 @@ WORDS_FLUX_PASS = 7             # the stage-1 share
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=1000, help="timed RK2 steps (the configuration runs 1000)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--n", type=int, default=4096)
@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-variant", action="store_true", help="skip the Float32 variant")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--start-steps", type=int, default=0,
+                    help="untimed steps on the measured simulator before the timed ones (profiling a developed flow)")
+    ap.add_argument("--cpu-budget", type=float, default=60.0,
+                    help="seconds of oracle stepping the reference arm may spend (it runs min(K, budget) steps)")
     return ap.parse_args()
 
 
@@ -161,8 +165,10 @@ def oracle_sim(sc, real_bytes=8):
     return o
 
 
-def cpu_rate(sc, warmup: int, steps: int | None, budget_s: float = 12.0):
-    """Oracle (the restated reference CPU path) on all host threads: cell-updates/s."""
+def cpu_rate(sc, warmup: int, steps: int | None, budget_s: float = 12.0, max_steps: int = 30):
+    """Oracle (the restated reference CPU path) on all host threads: cell-updates/s.
+
+    With steps=None the number of steps is chosen to fit budget_s (at most max_steps)."""
     from oracle import vf_oracle as O
     threads = O.set_threads(os.cpu_count() or 1)
     o = oracle_sim(sc)
@@ -172,7 +178,7 @@ def cpu_rate(sc, warmup: int, steps: int | None, budget_s: float = 12.0):
         t0 = time.perf_counter()
         o.perform_step(math.inf)
         one = time.perf_counter() - t0
-        steps = max(1, min(30, int(budget_s / max(one, 1e-6))))
+        steps = max(1, min(max_steps, int(budget_s / max(one, 1e-6))))
     t0 = time.perf_counter()
     for _ in range(steps):
         o.perform_step(math.inf)
@@ -191,8 +197,9 @@ def run_reference(args):
         return
     from volumefluxes_sm103 import scenarios
     sc = scenarios.hills_wet_dry(args.n)
-    value, threads, steps, el = cpu_rate(sc, args.warmup, args.steps)
-    sample = f"{steps} full RK2 steps of the {sc.nx}x{sc.ny} Float64 workload after {args.warmup} warm-up steps"
+    value, threads, steps, el = cpu_rate(sc, args.warmup, None, budget_s=args.cpu_budget, max_steps=args.steps)
+    sample = (f"{steps} full RK2 steps (of {args.steps} requested; time budget {args.cpu_budget:.0f} s) of the "
+              f"{sc.nx}x{sc.ny} Float64 workload from its initial state after {args.warmup} warm-up steps")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": steps, "warmup": args.warmup, "ms_per_step": el / steps * 1e3, "higher_is_better": True,
@@ -206,15 +213,19 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def measure_gpu(sc, dtype, args, world, local, lib_time=True):
+def measure_gpu(sc, dtype, args, world, local):
     import ctypes as C
     import volumefluxes_sm103 as vf
     real = np.float64 if dtype == "f64" else np.float32
+    ms = C.c_float()
+    if args.warmup > 0:  # warm-up on a throwaway simulator; the timed run starts from the initial state
+        warm = sc.build(vf.SM103Backend(real, device=local))
+        vf._native.check(warm._lib, warm.handle, warm._lib.vf_time_steps(warm.handle, args.warmup, C.byref(ms)))
+        warm.close()
     sim = sc.build(vf.SM103Backend(real, device=local))
     lib = sim._lib
-    ms = C.c_float()
-    if args.warmup > 0:
-        vf._native.check(lib, sim.handle, lib.vf_time_steps(sim.handle, args.warmup, C.byref(ms)))
+    if args.start_steps > 0:
+        vf._native.check(lib, sim.handle, lib.vf_time_steps(sim.handle, args.start_steps, C.byref(ms)))
     # headline: K steps back to back, CUDA events on the library's stream
     barrier(world)
     n0 = sim.launch_count()
@@ -223,9 +234,14 @@ def measure_gpu(sc, dtype, args, world, local, lib_time=True):
     launches = sim.launch_count() - n0
     barrier(world)
     ms_total = allmax(world, float(ms.value))
-    # per-kernel durations (events between the two kernels of every step)
+    # per-kernel durations (events between the two kernels of every step), on a
+    # second run over the same steps from the same initial state
+    prof = sc.build(vf.SM103Backend(real, device=local))
+    if args.start_steps > 0:
+        vf._native.check(lib, prof.handle, lib.vf_time_steps(prof.handle, args.start_steps, C.byref(ms)))
     mf, mst = C.c_float(), C.c_float()
-    vf._native.check(lib, sim.handle, lib.vf_time_kernels(sim.handle, args.steps, C.byref(mf), C.byref(mst)))
+    vf._native.check(lib, prof.handle, lib.vf_time_kernels(prof.handle, args.steps, C.byref(mf), C.byref(mst)))
+    prof.close()
     return sim, ms_total, mf.value / args.steps, mst.value / args.steps, launches, clk.summary()
 
 

@@ -303,9 +303,15 @@ int vf_create(const vf_config* cfg, vf_handle** out) {
   fill_geom(h, h->af.g);
   fill_phys(h, h->af.p);
   h->ad.rk2 = h->af.rk2 = cfg->stepper == VF_STEPPER_RK2;
-  // VF_KERNELS=tile selects the shared-memory tile kernels (kept for comparison).
-  const char* kv = std::getenv("VF_KERNELS");
-  h->ad.variant = h->af.variant = (kv && std::strcmp(kv, "tile") == 0) ? 1 : 0;
+  // Default kernels per precision: shared-memory tiles for Float64 (full warps on the
+  // 1/64-rate FP64 pipe), column marching for Float32 (fewest instructions per cell).
+  // VF_KERNELS=tile|march overrides.
+  h->ad.variant = 1;
+  h->af.variant = 0;
+  if (const char* kv = std::getenv("VF_KERNELS")) {
+    if (std::strcmp(kv, "tile") == 0) h->ad.variant = h->af.variant = 1;
+    if (std::strcmp(kv, "march") == 0) h->ad.variant = h->af.variant = 0;
+  }
   h->ad.B = static_cast<const double*>(h->B);
   h->ad.L = static_cast<double*>(h->L);
   h->ad.S = static_cast<double*>(h->S);
