@@ -148,6 +148,36 @@ int vf_time_steps(vf_handle* h, int64_t n_steps, float* ms_out);
  * of the stage (RK2) or apply (forward Euler) passes. */
 int vf_time_kernels(vf_handle* h, int64_t n_steps, float* ms_flux, float* ms_stage);
 
+/* Largest interior row count vf_water_volume_static accepts. */
+#define VF_STATIC_MAX_ROWS 16384
+
+/* Water volume sum((w - B_cell) * dx * dy) of a state the caller owns on the
+ * device, for callers that cannot let a library allocate device memory (code
+ * whose device memory belongs to another allocator that must account for
+ * every byte, such as CUDA.jl's pool, or loops that cannot afford the
+ * synchronisation cudaMalloc may imply). It calls no cudaMalloc/cudaFree:
+ * inputs and the output are the caller's, and its scratch (one Float64
+ * partial sum per interior row) is a fixed file-scope device array of
+ * VF_STATIC_MAX_ROWS doubles (128 KiB) that every GPU using the library holds
+ * until the process exits. No counterpart in the reference: an addition for
+ * allocation-free callers.
+ *
+ *  state_dev  dense reference-layout volume on the device, (nx+2gc) x (ny+2gc)
+ *             x 3, x fastest; only the w plane is read
+ *  B_dev      dense corner array (nx+2gc+1) x (ny+2gc+1), or NULL when
+ *             bottom_is_constant
+ *  out_dev    device double receiving the volume; written asynchronously on
+ *             `stream` (a cudaStream_t, NULL for the default stream)
+ *
+ * Returns VF_EINVAL for ny > VF_STATIC_MAX_ROWS or bad arguments (message
+ * from vf_last_error(NULL)). All calls share the scratch array, which keeps the
+ * last call's contents: calls whose kernels overlap on the GPU race. The first
+ * call on a device looks the array up with cudaGetSymbolAddress; make it before
+ * any stream capture. */
+int vf_water_volume_static(const void* state_dev, const void* B_dev, int32_t nx, int32_t ny, int32_t gc,
+                           int32_t real_bytes, double dx, double dy, int32_t bottom_is_constant,
+                           double bottom_constant, double* out_dev, void* stream);
+
 /* Message for the last failure on this handle (or of vf_create when h is NULL). */
 const char* vf_last_error(vf_handle* h);
 /* Kernel launches issued by this handle since creation. */

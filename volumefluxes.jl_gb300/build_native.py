@@ -1,11 +1,12 @@
 """Build libvfsm103.so, the sm_103a shallow-water step library, in-tree.
 
-Three translation units compile in parallel with nvcc and link into one shared
+Four translation units compile in parallel with nvcc and link into one shared
 library with the CUDA runtime linked statically:
 
   vf_f64.cu  Float64 kernels, -fmad=false (each operation rounds as in Julia)
   vf_f32.cu  Float32 kernels, contraction and fast division allowed
   vf_abi.cu  the extern "C" boundary of include/volumefluxes_sm103.h
+  vf_noalloc.cu  the allocation-free water-volume entry point
 
 Usage: python volumefluxes.jl_gb300/build_native.py [--force]
 """
@@ -31,6 +32,7 @@ UNITS = {
     "vf_f64.cu": ["-fmad=false"],
     "vf_f32.cu": ["-fmad=true", "-ftz=true", "-prec-sqrt=false"],
     "vf_abi.cu": [],
+    "vf_noalloc.cu": [],
 }
 
 

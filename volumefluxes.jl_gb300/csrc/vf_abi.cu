@@ -25,6 +25,10 @@ long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
 
 }  // namespace
 
+namespace vf {
+void set_global_error(const char* msg) { g_create_error = msg; }
+}  // namespace vf
+
 struct vf_handle {
   vf_config cfg;
   int device = 0;

@@ -27,7 +27,9 @@ EXPORTED_SYMBOLS = (
     "vf_create", "vf_destroy", "vf_upload_bottom", "vf_set_interior_state", "vf_upload_state",
     "vf_download_state", "vf_get_interior_state", "vf_step", "vf_simulate", "vf_water_volume",
     "vf_device_state", "vf_stream", "vf_time_steps", "vf_time_kernels", "vf_last_error", "vf_launch_count",
+    "vf_water_volume_static",
 )
+VF_STATIC_MAX_ROWS = 16384
 
 
 class VfConfig(C.Structure):
@@ -98,6 +100,9 @@ def load(build_if_missing: bool = False):
         "vf_time_steps": (C.c_int, [H, C.c_int64, C.POINTER(C.c_float)]),
         "vf_time_kernels": (C.c_int, [H, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "vf_last_error": (C.c_char_p, [H]),
+        "vf_water_volume_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                             C.c_double, C.c_double, C.c_int32, C.c_double, C.c_void_p,
+                                             C.c_void_p]),
         "vf_launch_count": (C.c_int64, [H]),
     }
     for name, (res, args) in sig.items():
