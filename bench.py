@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--start-steps", type=int, default=0,
                     help="untimed steps on the measured simulator before the timed ones (profiling a developed flow)")
+    ap.add_argument("--state-out", default=None,
+                    help="save the measured simulator's interior state (after --start-steps) to this .npz and exit")
+    ap.add_argument("--state-in", default=None, help="start from an interior state saved with --state-out")
     ap.add_argument("--cpu-budget", type=float, default=60.0,
                     help="seconds of oracle stepping the reference arm may spend (it runs min(K, budget) steps)")
     return ap.parse_args()
@@ -68,17 +71,31 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_table():
-    """dram bytes per interior cell per launch, from the committed ncu summaries."""
+def profile_table(tag: str):
+    """Per-cell figures from the committed ncu summaries: lines '<tag>: <pass> <dtype> <value>'."""
     out = {}
     for f in sorted((ROOT / "profiles").glob("*.md")):
         for line in f.read_text().splitlines():
-            if line.startswith("traffic:"):
+            if line.startswith(tag + ":"):
                 parts = line.split()
-                # traffic: <kernel> <dtype> <bytes_per_cell>
                 if len(parts) == 4:
                     out[(parts[1], parts[2])] = float(parts[3])
     return out
+
+
+def kernel_names(dtype: str) -> dict:
+    """Kernels the library runs for this precision (tiles for Float64, marching for Float32, VF_KERNELS overrides)."""
+    variant = os.environ.get("VF_KERNELS", "tile" if dtype == "f64" else "march")
+    t = "double" if dtype == "f64" else "float"
+    if variant == "march":
+        return {"flux": f"k_flux_march<{t},64>", "stage": f"k_stage_march<{t},64>"}
+    return {"flux": f"k_flux<{t}>", "stage": f"k_stage2<{t}>"}
+
+
+# FP64 pipe peak: 2 DFMA-class thread instructions per clock per SM (ncu's
+# sm__sass_thread_inst_executed_op_dfma_pred_on.peak_sustained on GB300), 152 SMs.
+FP64_INST_PER_CLK_SM = 2.0
+N_SMS = 152
 
 
 class Clocks:
@@ -226,6 +243,10 @@ def measure_gpu(sc, dtype, args, world, local):
     lib = sim._lib
     if args.start_steps > 0:
         vf._native.check(lib, sim.handle, lib.vf_time_steps(sim.handle, args.start_steps, C.byref(ms)))
+    if args.state_out:
+        st = vf.current_interior_state(sim)
+        np.savez(args.state_out, h=st.h, hu=st.hu, hv=st.hv)
+        sys.exit(0)
     # headline: K steps back to back, CUDA events on the library's stream
     barrier(world)
     n0 = sim.launch_count()
@@ -270,16 +291,31 @@ def e2e_rate(sim, steps: int):
 def roofline(sc, dtype, ms_flux, ms_stage, peak, peak_kind, traffic):
     e = 8 if dtype == "f64" else 4
     cells = sc.nx * sc.ny
-    dom_name, dom_ms, words = ("k_stage2", ms_stage, WORDS_STAGE_PASS) if ms_stage >= ms_flux else \
-        ("k_flux", ms_flux, WORDS_FLUX_PASS)
+    which, dom_ms, words = ("stage", ms_stage, WORDS_STAGE_PASS) if ms_stage >= ms_flux else \
+        ("flux", ms_flux, WORDS_FLUX_PASS)
     alg = words * e * cells
     ach = alg / (dom_ms * 1e-3) / 1e9
-    tb = traffic.get((dom_name, dtype))
+    tb = traffic.get((which, dtype))
     return {
-        "bound": "hbm", "kernel": dom_name, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-        "peak_kind": peak_kind, "traffic": (tb * cells) if tb is not None else None,
+        "bound": "hbm", "kernel": kernel_names(dtype)[which], "achieved": ach, "peak": peak, "unit": "GB/s",
+        "frac": ach / peak, "peak_kind": peak_kind, "traffic": (tb * cells) if tb is not None else None,
+        "traffic_source": "ncu dram bytes per cell of a 3072^2 developed-flow capture, scaled to this launch"
+                          if tb is not None else None,
         "algorithmic_bytes": alg, "launch_ms": dom_ms,
     }
+
+
+def fp64_roofline(sc, ms_flux, ms_stage, clk_mhz, inst):
+    """Compute bound of the Float64 kernels: FP64-pipe thread instructions per second vs the pipe's peak."""
+    n = inst.get(("stage", "f64"))
+    if n is None:
+        return None
+    cells = sc.nx * sc.ny
+    ach = n * cells / (ms_stage * 1e-3)
+    peak = FP64_INST_PER_CLK_SM * N_SMS * (clk_mhz or 2070.0) * 1e6
+    return {"bound": "fp64_pipe", "kernel": kernel_names("f64")["stage"], "achieved": ach, "peak": peak,
+            "unit": "FP64 thread-inst/s", "frac": ach / peak, "inst_per_cell": n,
+            "inst_source": "ncu DADD+DMUL+DFMA per cell, 3072^2 developed-flow capture"}
 
 
 def main():
@@ -290,8 +326,12 @@ def main():
     world, rank, local = dist_setup("nccl")
     from volumefluxes_sm103 import scenarios
     sc = scenarios.hills_wet_dry(args.n)
+    if args.state_in:
+        d = np.load(args.state_in)
+        sc.w0, sc.hu0, sc.hv0 = d["h"], d["hu"], d["hv"]
     peak, peak_kind = peaks()
-    traffic = traffic_table()
+    traffic = profile_table("traffic")
+    fp64_inst = profile_table("fp64_inst_per_cell")
     cells = sc.nx * sc.ny
     dtypes = [args.dtype] + ([] if args.no_variant else [d for d in ("f64", "f32") if d != args.dtype])
     results = {}
@@ -310,9 +350,12 @@ def main():
             "roofline": roofline(sc, dt, ms_flux, ms_stage, peak, peak_kind, traffic),
             "roofline_step": {"bound": "hbm", "achieved": step_ach, "peak": peak, "unit": "GB/s",
                               "frac": step_ach / peak, "words_per_cell": WORDS_PER_CELL_STEP},
-            "kernel_ms": {"k_flux": ms_flux, "k_stage2": ms_stage},
+            "kernel_ms": {kernel_names(dt)["flux"]: ms_flux, kernel_names(dt)["stage"]: ms_stage},
             "e2e": {"value": e2e_v, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         }
+        if dt == "f64":
+            results[dt]["compute_roofline"] = fp64_roofline(sc, ms_flux, ms_stage, (clk or {}).get("sm_mhz"),
+                                                            fp64_inst)
         sim.close()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -331,6 +374,7 @@ def main():
                    "seed": sc.meta["seed"], "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (state %.0f MB per volume)" % (3 * cells * (8 if args.dtype == 'f64' else 4) / 1e6)},
         "roofline": head["roofline"], "roofline_step": head["roofline_step"], "kernel_ms": head["kernel_ms"],
+        "compute_roofline": head.get("compute_roofline"),
         "cpu_baseline": cpu, "e2e": head["e2e"], "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
         "variants": {k: v for k, v in results.items() if k != args.dtype},
     }

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define VF_ABI_VERSION 1
+#define VF_ABI_VERSION 2
 #define VF_MAX_SOURCES 8
 
 /* Error codes. */
@@ -44,6 +44,12 @@ extern "C" {
 #define VF_SRC_BOTTOM 1       /* SourceTermBottom, src/sourceterms/source_term_bottom.jl:24-41 */
 #define VF_SRC_CONST_RAIN 2   /* ConstantRain(rate [m/h]), src/sourceterms/source_term_rain.jl:24-30,71-76 */
 #define VF_SRC_CONST_INFIL 3  /* ConstantInfiltration(rate [m/s]), src/sourceterms/source_term_infiltration.jl:73-88 */
+#define VF_SRC_TIME_RAIN 4    /* TimeDependentRain(rates [m/h], times), src/sourceterms/source_term_rain.jl:32-54;
+                                 table from vf_set_source_table */
+#define VF_SRC_HORTON 5       /* HortonInfiltration: rate = fc, aux = (f0, k), per-cell factor from
+                                 vf_set_source_field, src/sourceterms/source_term_infiltration.jl:21-70 */
+#define VF_SRC_RAIN_FIELD 6   /* per-cell rain [m/s] from vf_set_source_field: FunctionalRain evaluated at
+                                 cell centres by the caller, src/sourceterms/source_term_rain.jl:57-76 */
 
 /* ImplicitFriction laws, src/friction.jl:30-43. */
 #define VF_FRICTION_NONE 0
@@ -54,7 +60,9 @@ extern "C" {
 #define VF_STEPPER_FE 1       /* ForwardEulerStepper, src/timestepper/forwardeuler.jl:23-47 */
 #define VF_STEPPER_RK2 2      /* RungeKutta2, src/timestepper/rungekutta.jl:21-52 */
 #define VF_BC_WALL 1          /* WallBC, src/bc.jl:81-110 */
+#define VF_BC_PERIODIC 2      /* PeriodicBC, src/bc.jl:29-40 */
 #define VF_REC_LINEAR 1       /* LinearReconstruction(theta), src/reconstruction/linearreconstruction.jl:22-102 */
+#define VF_REC_NONE 2         /* NoReconstruction, src/reconstruction/noreconstruction.jl:30-46 */
 
 /* Everything the reference's ConservedSystem + Simulator constructors carry
  * for this path (src/system.jl:37-53, src/simulator.jl:72-91,
@@ -65,15 +73,16 @@ typedef struct vf_config {
   double extent[4];          /* x0, x1, y0, y1 */
   int32_t real_bytes;        /* 8: Float64 state, 4: Float32 state */
   double g, rho, depth_cutoff, desingularizing_kappa;
-  int32_t reconstruction;    /* VF_REC_LINEAR */
+  int32_t reconstruction;    /* VF_REC_* */
   double theta;
   int32_t n_sources;
   int32_t source_kind[VF_MAX_SOURCES];
   double source_rate[VF_MAX_SOURCES];
+  double source_aux[VF_MAX_SOURCES][2];
   int32_t friction;          /* VF_FRICTION_* */
   double friction_Cz;
   int32_t stepper;           /* VF_STEPPER_* */
-  int32_t bc;                /* VF_BC_WALL */
+  int32_t bc;                /* VF_BC_* */
   double cfl;
   int32_t bottom_is_constant;/* 1: ConstantBottomTopography(bottom_constant) */
   double bottom_constant;
@@ -96,6 +105,17 @@ void vf_destroy(vf_handle* h);
  * x fastest. */
 int vf_upload_bottom(vf_handle* h, const void* B_corners);
 
+/* Data of the time- or cell-dependent source term at position `index` of the
+ * source list. vf_set_source_table: TimeDependentRain's n breakpoints `times`
+ * and rates `rates` [m/h] (the reference's constructor, src/sourceterms/
+ * source_term_rain.jl:35-41). vf_set_source_field: HortonInfiltration's factor
+ * (src/sourceterms/source_term_infiltration.jl:37-44) or a rain field [m/s]
+ * over the total grid (nx+2gc) x (ny+2gc), x fastest, in the real type. A
+ * field may be re-uploaded between steps (a FunctionalRain re-evaluated at the
+ * new time). */
+int vf_set_source_table(vf_handle* h, int32_t index, const double* times, const double* rates, int32_t n);
+int vf_set_source_field(vf_handle* h, int32_t index, const void* field);
+
 /* Stands in for set_current_state!(sim, state) (src/simulator.jl:119-135):
  * writes the interior planes (nx*ny each, x fastest), then the device
  * boundary update (src/bc.jl:81-110). */
@@ -110,10 +130,11 @@ int vf_download_state(vf_handle* h, void* state);
 int vf_get_interior_state(vf_handle* h, void* w, void* hu, void* hv);
 
 /* Stands in for perform_step!(sim, max_dt) (src/simulator.jl:145-177): one
- * full FE/RK2 step including friction, dry clamp and boundary update. Writes
- * the dt used (current_timestep) to *dt_out. Does not advance the handle's
- * time; the caller does t += dt as simulate_to_time does (src/simulator.jl:205). */
-int vf_step(vf_handle* h, double max_dt, double* dt_out);
+ * full FE/RK2 step including friction, dry clamp and boundary update, with
+ * time-dependent sources evaluated at t (the simulator's current time).
+ * Writes the dt used (current_timestep) to *dt_out. Does not advance t; the
+ * caller does t += dt as simulate_to_time does (src/simulator.jl:205). */
+int vf_step(vf_handle* h, double max_dt, double t, double* dt_out);
 
 /* Stands in for the loop of simulate_to_time (src/simulator.jl:179-212) with
  * the time kept on the device: from t0, step while t < endtime with

@@ -128,6 +128,43 @@ double cr_cbrt(double x) {
 inline float cr_cbrt(float x) { return (float)cr_cbrt((double)x); }
 
 // ---------------------------------------------------------------------------
+// Deterministic exp for HortonInfiltration: Cody-Waite reduction by ln 2 (split
+// in two doubles), Taylor polynomial of degree 14 in Horner form with fused
+// multiply-adds, exact scaling by 2^k. Only IEEE-exact operations, so the
+// device computes the same bits. Accurate to about one ulp of Julia's exp.
+double det_exp(double x) {
+  if (x != x) return x;
+  if (x > 709.782712893384) return std::numeric_limits<double>::infinity();
+  if (x < -745.1332191019412) return 0.0;
+  const double inv_ln2 = 0x1.71547652b82fep+0;
+  const double ln2_hi = 0x1.62e42fefa39efp-1, ln2_lo = 0x1.abc9e3b39803fp-56;
+  double kd = x * inv_ln2;
+  kd = (kd + 6755399441055744.0) - 6755399441055744.0;  // round to nearest integer
+  double r = std::fma(-kd, ln2_hi, x);
+  r = std::fma(-kd, ln2_lo, r);
+  static const double c[15] = {0x1.0000000000000p+0, 0x1.0000000000000p+0, 0x1.0000000000000p-1,
+                               0x1.5555555555555p-3, 0x1.5555555555555p-5, 0x1.1111111111111p-7,
+                               0x1.6c16c16c16c17p-10, 0x1.a01a01a01a01ap-13, 0x1.a01a01a01a01ap-16,
+                               0x1.71de3a556c734p-19, 0x1.27e4fb7789f5cp-22, 0x1.ae64567f544e4p-26,
+                               0x1.1eed8eff8d898p-29, 0x1.6124613a86d09p-33, 0x1.93974a8c07c9dp-37};
+  double p = c[14];
+  for (int n = 13; n >= 0; --n) p = std::fma(p, r, c[n]);
+  int k = (int)kd;
+  // p * 2^k with one rounding at most (only for subnormal results)
+  if (k > 1023) { p = p * 2.0; k -= 1; }
+  if (k < -1022) {
+    const uint64_t b = (uint64_t)(k + 54 + 1023) << 52;
+    double s1;
+    std::memcpy(&s1, &b, 8);
+    return (p * s1) * 0x1p-54;
+  }
+  const uint64_t b = (uint64_t)(k + 1023) << 52;
+  double s2;
+  std::memcpy(&s2, &b, 8);
+  return p * s2;
+}
+
+// ---------------------------------------------------------------------------
 template <typename T>
 struct Sim {
   vfo_params p;
@@ -138,6 +175,8 @@ struct Sim {
   // State buffers U[0..nsub]; left/right face buffers; wavespeed scalar field.
   std::vector<std::vector<T>> U;
   std::vector<T> left, right, ws;
+  std::vector<double> src_times[VFO_MAX_SOURCES], src_rates[VFO_MAX_SOURCES];
+  std::vector<T> src_field[VFO_MAX_SOURCES];  // Horton factor or rain field, total grid
   double t;
   double current_dt;
   // Equation constants in the state's real type.
@@ -253,7 +292,31 @@ struct Ops {
   // --- src/reconstruction/linearreconstruction.jl:58-102 -------------------
   // for_each_inner_cell(...; ghostcells=1): along dir, cells 1..N-2 (0-based);
   // across, the interior (src/grid.jl:213-244).
+  // --- src/reconstruction/noreconstruction.jl:30-46 ------------------------
+  void reconstruct_none(const std::vector<T>& Uin) {
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < s.N2; ++j) {
+      for (int i = 0; i < s.N1; ++i) {
+        for (int k = 0; k < 3; ++k) {
+          at(s.left, k, i, j) = at(Uin, k, i, j);
+          at(s.right, k, i, j) = at(Uin, k, i, j);
+        }
+      }
+    }
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < s.N2; ++j) {
+      for (int i = 0; i < s.N1; ++i) {
+        at(s.left, 0, i, j) = at(Uin, 0, i, j) - Bc(i, j);
+        at(s.right, 0, i, j) = at(Uin, 0, i, j) - Bc(i, j);
+      }
+    }
+  }
+
   void reconstruct(const std::vector<T>& Uin, int dir) {
+    if (s.p.reconstruction == VFO_REC_NONE) {
+      reconstruct_none(Uin);
+      return;
+    }
     const int gc = s.p.gc;
     const int ilo = dir == 0 ? 1 : gc, ihi = dir == 0 ? s.N1 - 1 : gc + s.p.nx;
     const int jlo = dir == 0 ? gc : 1, jhi = dir == 0 ? gc + s.p.ny : s.N2 - 1;
@@ -336,8 +399,39 @@ struct Ops {
     }
   }
 
+  // TimeDependentRain, src/sourceterms/source_term_rain.jl:45-54
+  double table_rain(int n, double t) const {
+    const std::vector<double>& tt = s.src_times[n];
+    const std::vector<double>& rr = s.src_rates[n];
+    size_t idx = 0;
+    while (idx + 1 < tt.size()) {
+      if (t < tt[idx + 1]) break;
+      ++idx;
+    }
+    return rr[idx] / 3600;
+  }
+
+  // HortonInfiltration, src/sourceterms/source_term_infiltration.jl:68-70,83-88
+  void horton(std::vector<T>& out, int n, double t) {
+    const T fc = (T)s.p.source_rate[n], f0 = (T)s.p.source_aux[n][0], k = (T)s.p.source_aux[n][1];
+    const T decay = (T)det_exp((double)(-k * (T)t));
+    const T rate = fc + (f0 - fc) * decay;
+    const std::vector<T>& f = s.src_field[n];
+    const size_t m = s.plane;
+#pragma omp parallel for schedule(static)
+    for (long long c = 0; c < (long long)m; ++c) out[c] = out[c] - f[c] * rate;
+  }
+
+  // FunctionalRain evaluated at cell centres by the caller, source_term_rain.jl:65-76
+  void rain_field(std::vector<T>& out, int n) {
+    const std::vector<T>& f = s.src_field[n];
+    const size_t m = s.plane;
+#pragma omp parallel for schedule(static)
+    for (long long c = 0; c < (long long)m; ++c) out[c] = out[c] + f[c];
+  }
+
   // --- src/system.jl:62-75 -------------------------------------------------
-  void add_time_derivative(std::vector<T>& out, const std::vector<T>& Uin, T* maxspeed) {
+  void add_time_derivative(std::vector<T>& out, const std::vector<T>& Uin, T* maxspeed, double t) {
     for (int dir = 0; dir < 2; ++dir) {
       reconstruct(Uin, dir);
       maxspeed[dir] = compute_flux(out, dir);
@@ -345,10 +439,14 @@ struct Ops {
         if (s.p.source_kind[n] == VFO_SRC_BOTTOM) bottom_source(out, dir);
     }
     for (int n = 0; n < s.p.n_sources; ++n) {
-      if (s.p.source_kind[n] == VFO_SRC_CONST_RAIN)
-        add_all_cells_h(out, (T)(s.p.source_rate[n] / 3600), false);
-      else if (s.p.source_kind[n] == VFO_SRC_CONST_INFIL)
-        add_all_cells_h(out, (T)s.p.source_rate[n], true);
+      switch (s.p.source_kind[n]) {
+        case VFO_SRC_CONST_RAIN: add_all_cells_h(out, (T)(s.p.source_rate[n] / 3600), false); break;
+        case VFO_SRC_CONST_INFIL: add_all_cells_h(out, (T)s.p.source_rate[n], true); break;
+        case VFO_SRC_TIME_RAIN: add_all_cells_h(out, (T)table_rain(n, t), false); break;
+        case VFO_SRC_HORTON: horton(out, n, t); break;
+        case VFO_SRC_RAIN_FIELD: rain_field(out, n); break;
+        default: break;
+      }
     }
   }
 
@@ -402,8 +500,34 @@ struct Ops {
     }
   }
 
-  // --- src/bc.jl:81-110 ----------------------------------------------------
+  // --- src/bc.jl:29-40 -----------------------------------------------------
+  void update_bc_periodic(std::vector<T>& d) {
+    const int gc = s.p.gc, N1 = s.N1, N2 = s.N2;
+    for (int j = gc; j < gc + s.p.ny; ++j) {
+      for (int g = 1; g <= gc; ++g) {
+        for (int k = 0; k < 3; ++k) {
+          at(d, k, g - 1, j) = at(d, k, N1 + g - 2 * gc - 1, j);
+          at(d, k, N1 - (gc - g) - 1, j) = at(d, k, gc + g - 1, j);
+        }
+      }
+    }
+    for (int g = 1; g <= gc; ++g) {
+      for (int i = gc; i < gc + s.p.nx; ++i) {
+        for (int k = 0; k < 3; ++k) {
+          at(d, k, i, g - 1) = at(d, k, i, N2 + g - 2 * gc - 1);
+          at(d, k, i, N2 - (gc - g) - 1) = at(d, k, i, gc + g - 1);
+        }
+      }
+    }
+  }
+
   void update_bc(std::vector<T>& d) {
+    if (s.p.bc == VFO_BC_PERIODIC) update_bc_periodic(d);
+    else update_bc_wall(d);
+  }
+
+  // --- src/bc.jl:81-110 ----------------------------------------------------
+  void update_bc_wall(std::vector<T>& d) {
     const int gc = s.p.gc, N1 = s.N1, N2 = s.N2;
     // X: ghost columns at interior rows.
     for (int j = gc; j < gc + s.p.ny; ++j) {
@@ -431,7 +555,7 @@ struct Ops {
     const std::vector<T>& cur = s.U[s_idx];
     std::fill(out.begin(), out.end(), (T)0);
     T speed[2];
-    add_time_derivative(out, cur, speed);
+    add_time_derivative(out, cur, speed, s.t);
     if (s_idx == 0) {
       // timestep_computer, src/simulator.jl:147-150
       const double dxs = s.dx / (double)speed[0];
@@ -499,7 +623,8 @@ int check_params(const vfo_params* p, const double* B) {
   if (p->nx < 2 || p->ny < 2 || p->gc < 2) return -1;
   if (p->real_bytes != 8 && p->real_bytes != 4) return -1;
   if (p->stepper != VFO_STEPPER_FE && p->stepper != VFO_STEPPER_RK2) return -1;
-  if (p->bc != VFO_BC_WALL || p->reconstruction != VFO_REC_LINEAR) return -1;
+  if (p->bc != VFO_BC_WALL && p->bc != VFO_BC_PERIODIC) return -1;
+  if (p->reconstruction != VFO_REC_LINEAR && p->reconstruction != VFO_REC_NONE) return -1;
   if (p->n_sources < 0 || p->n_sources > VFO_MAX_SOURCES) return -1;
   if (!p->bottom_is_constant && !B) return -1;
   return 0;
@@ -666,7 +791,7 @@ int vfo_update_bc_wall(double* state, int nx, int ny, int gc) {
   if (!state || nx < gc || ny < gc || gc < 1) return -1;
   Sim<double> s;
   std::memset(&s.p, 0, sizeof(s.p));
-  s.p.nx = nx; s.p.ny = ny; s.p.gc = gc;
+  s.p.nx = nx; s.p.ny = ny; s.p.gc = gc; s.p.bc = VFO_BC_WALL;
   s.N1 = nx + 2 * gc; s.N2 = ny + 2 * gc;
   s.plane = (size_t)s.N1 * s.N2;
   std::vector<double> d(state, state + 3 * s.plane);
@@ -676,6 +801,43 @@ int vfo_update_bc_wall(double* state, int nx, int ny, int gc) {
 }
 
 double vfo_cbrt(double x) { return cr_cbrt(x); }
+
+double vfo_exp(double x) { return det_exp(x); }
+
+int vfo_set_source_table(vfo_sim* sim, int index, const double* times, const double* rates, int n) {
+  Handle* h = reinterpret_cast<Handle*>(sim);
+  if (!h || index < 0 || index >= VFO_MAX_SOURCES || n < 1 || !times || !rates) return -1;
+  auto set = [&](auto* S) {
+    S->src_times[index].assign(times, times + n);
+    S->src_rates[index].assign(rates, rates + n);
+  };
+  if (h->d) set(h->d); else set(h->f);
+  return 0;
+}
+
+int vfo_set_source_field(vfo_sim* sim, int index, const double* field) {
+  Handle* h = reinterpret_cast<Handle*>(sim);
+  if (!h || index < 0 || index >= VFO_MAX_SOURCES || !field) return -1;
+  auto set = [&](auto* S) {
+    S->src_field[index].resize(S->plane);
+    for (size_t c = 0; c < S->plane; ++c) S->src_field[index][c] = (decltype(S->src_field[index][0] + 0))field[c];
+  };
+  if (h->d) set(h->d); else set(h->f);
+  return 0;
+}
+
+int vfo_update_bc_periodic(double* state, int nx, int ny, int gc) {
+  if (!state || nx < gc || ny < gc || gc < 1) return -1;
+  Sim<double> s;
+  std::memset(&s.p, 0, sizeof(s.p));
+  s.p.nx = nx; s.p.ny = ny; s.p.gc = gc; s.p.bc = VFO_BC_PERIODIC;
+  s.N1 = nx + 2 * gc; s.N2 = ny + 2 * gc;
+  s.plane = (size_t)s.N1 * s.N2;
+  std::vector<double> d(state, state + 3 * s.plane);
+  Ops<double>(s).update_bc(d);
+  std::memcpy(state, d.data(), 3 * s.plane * sizeof(double));
+  return 0;
+}
 
 double vfo_desingularize(double h, double kappa) {
   Sim<double> s;

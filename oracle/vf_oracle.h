@@ -24,13 +24,18 @@ extern "C" {
 enum {
   VFO_SRC_BOTTOM = 1,        /* SourceTermBottom, src/sourceterms/source_term_bottom.jl:24-41 */
   VFO_SRC_CONST_RAIN = 2,    /* ConstantRain(rate in m/h), source_term_rain.jl:24-30,71-76 */
-  VFO_SRC_CONST_INFIL = 3    /* ConstantInfiltration(rate in m/s), source_term_infiltration.jl:73-88 */
+  VFO_SRC_CONST_INFIL = 3,   /* ConstantInfiltration(rate in m/s), source_term_infiltration.jl:73-88 */
+  VFO_SRC_TIME_RAIN = 4,     /* TimeDependentRain(rates [m/h], times), source_term_rain.jl:32-54 (table set later) */
+  VFO_SRC_HORTON = 5,        /* HortonInfiltration: rate=fc, aux0=f0, aux1=k, per-cell factor set later,
+                                source_term_infiltration.jl:21-70 */
+  VFO_SRC_RAIN_FIELD = 6     /* per-cell rain rate [m/s] over the total grid (FunctionalRain evaluated
+                                by the caller at cell centres), source_term_rain.jl:57-68 */
 };
 
 enum { VFO_FRICTION_NONE = 0, VFO_FRICTION_BSA2012 = 1, VFO_FRICTION_FCG2016 = 2, VFO_FRICTION_BH2021 = 3 };
 enum { VFO_STEPPER_FE = 1, VFO_STEPPER_RK2 = 2 };
-enum { VFO_BC_WALL = 1 };
-enum { VFO_REC_LINEAR = 1 };
+enum { VFO_BC_WALL = 1, VFO_BC_PERIODIC = 2 };
+enum { VFO_REC_LINEAR = 1, VFO_REC_NONE = 2 };
 enum { VFO_MAX_SOURCES = 8 };
 
 typedef struct {
@@ -43,6 +48,7 @@ typedef struct {
   int n_sources;
   int source_kind[VFO_MAX_SOURCES];
   double source_rate[VFO_MAX_SOURCES];
+  double source_aux[VFO_MAX_SOURCES][2];
   int friction;              /* VFO_FRICTION_* */
   double friction_Cz;
   int stepper;               /* VFO_STEPPER_* */
@@ -57,6 +63,13 @@ typedef struct vfo_sim vfo_sim;
 /* B_corners: (nx+2gc+1)*(ny+2gc+1) doubles, ignored when bottom_is_constant. */
 int vfo_create(const vfo_params* p, const double* B_corners, vfo_sim** out);
 void vfo_destroy(vfo_sim* s);
+/* Tables and per-cell arrays of source term `index` (its position in the
+ * source list): TimeDependentRain times/rates (n entries); HortonInfiltration
+ * factor or rain field over the total grid (nx+2gc)*(ny+2gc), x fastest. */
+int vfo_set_source_table(vfo_sim* s, int index, const double* times, const double* rates, int n);
+int vfo_set_source_field(vfo_sim* s, int index, const double* field);
+/* The deterministic exp used for Horton infiltration (identical on the device). */
+double vfo_exp(double x);
 /* Interior planes, nx*ny each, x fastest; then the boundary update
  * (src/simulator.jl:119-135). */
 int vfo_set_interior(vfo_sim* s, const double* w, const double* hu, const double* hv);
@@ -84,6 +97,8 @@ double vfo_minmod_slope(double l, double c, double r, double theta);
 double vfo_bottom_lookup(const double* B, int n1p1, int n2p1, int i, int j, int which);
 /* Wall boundary update in place on a full 3-plane state. */
 int vfo_update_bc_wall(double* state, int nx, int ny, int gc);
+/* Periodic boundary update in place on a full 3-plane state. */
+int vfo_update_bc_periodic(double* state, int nx, int ny, int gc);
 double vfo_cbrt(double x);
 double vfo_desingularize(double h, double kappa);
 

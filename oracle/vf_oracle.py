@@ -14,7 +14,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "libvforacle.so"
 
-SRC_BOTTOM, SRC_CONST_RAIN, SRC_CONST_INFIL = 1, 2, 3
+SRC_BOTTOM, SRC_CONST_RAIN, SRC_CONST_INFIL, SRC_TIME_RAIN, SRC_HORTON, SRC_RAIN_FIELD = 1, 2, 3, 4, 5, 6
+BC_WALL, BC_PERIODIC = 1, 2
+REC_LINEAR, REC_NONE = 1, 2
 FRICTION_NONE, FRICTION_BSA2012, FRICTION_FCG2016, FRICTION_BH2021 = 0, 1, 2, 3
 STEPPER_FE, STEPPER_RK2 = 1, 2
 
@@ -27,6 +29,7 @@ class Params(C.Structure):
         ("g", C.c_double), ("rho", C.c_double), ("depth_cutoff", C.c_double), ("desingularizing_kappa", C.c_double),
         ("reconstruction", C.c_int), ("theta", C.c_double),
         ("n_sources", C.c_int), ("source_kind", C.c_int * 8), ("source_rate", C.c_double * 8),
+        ("source_aux", (C.c_double * 2) * 8),
         ("friction", C.c_int), ("friction_Cz", C.c_double),
         ("stepper", C.c_int), ("bc", C.c_int), ("cfl", C.c_double),
         ("bottom_is_constant", C.c_int), ("bottom_constant", C.c_double),
@@ -67,6 +70,10 @@ def load():
         "vfo_bottom_lookup": (D, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
         "vfo_update_bc_wall": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
         "vfo_cbrt": (D, [D]),
+        "vfo_exp": (D, [D]),
+        "vfo_set_source_table": (C.c_int, [P, C.c_int, P, P, C.c_int]),
+        "vfo_set_source_field": (C.c_int, [P, C.c_int, P]),
+        "vfo_update_bc_periodic": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
         "vfo_desingularize": (D, [D, D]),
     }
     for n, (r, a) in sig.items():
@@ -86,7 +93,9 @@ class OracleSim:
 
     def __init__(self, *, nx, ny, extent=((0.0, 1.0), (0.0, 1.0)), real_bytes=8, g=9.81, rho=1.0,
                  depth_cutoff=1e-5, desingularizing_kappa=1e-5, theta=1.2, sources=(), friction=FRICTION_NONE,
-                 friction_Cz=0.0, stepper=STEPPER_RK2, cfl=0.25, B=None, bottom_constant=0.0, gc=2):
+                 friction_Cz=0.0, stepper=STEPPER_RK2, cfl=0.25, B=None, bottom_constant=0.0, gc=2, bc=BC_WALL,
+                 reconstruction=REC_LINEAR):
+        """sources: list of (kind, rate) or (kind, rate, aux0, aux1)."""
         self.lib = load()
         p = Params()
         p.nx, p.ny, p.gc = nx, ny, gc
@@ -95,12 +104,14 @@ class OracleSim:
             p.extent[i] = e[i]
         p.real_bytes = real_bytes
         p.g, p.rho, p.depth_cutoff, p.desingularizing_kappa = g, rho, depth_cutoff, desingularizing_kappa
-        p.reconstruction, p.theta = 1, theta
+        p.reconstruction, p.theta = reconstruction, theta
         p.n_sources = len(sources)
-        for i, (k, r) in enumerate(sources):
-            p.source_kind[i], p.source_rate[i] = k, r
+        for i, src in enumerate(sources):
+            p.source_kind[i], p.source_rate[i] = src[0], src[1]
+            if len(src) > 2:
+                p.source_aux[i][0], p.source_aux[i][1] = src[2], src[3]
         p.friction, p.friction_Cz = friction, friction_Cz
-        p.stepper, p.bc, p.cfl = stepper, 1, cfl
+        p.stepper, p.bc, p.cfl = stepper, bc, cfl
         self.nx, self.ny, self.gc = nx, ny, gc
         self.N1, self.N2 = nx + 2 * gc, ny + 2 * gc
         if B is None:
@@ -124,6 +135,17 @@ class OracleSim:
                 self.lib.vfo_destroy(self.h)
         except Exception:
             pass
+
+    def set_source_table(self, index, times, rates):
+        t = np.ascontiguousarray(times, dtype=np.float64)
+        r = np.ascontiguousarray(rates, dtype=np.float64)
+        assert self.lib.vfo_set_source_table(self.h, index, _p(t), _p(r), len(t)) == 0
+
+    def set_source_field(self, index, field):
+        """field: (N1, N2) array over the total grid, indexed [i, j]."""
+        f = np.ascontiguousarray(np.asarray(field, dtype=np.float64).T)
+        assert f.shape == (self.N2, self.N1)
+        assert self.lib.vfo_set_source_field(self.h, index, _p(f)) == 0
 
     def set_interior(self, w, hu, hv):
         planes = [np.ascontiguousarray(np.asarray(a, dtype=np.float64).T) for a in (w, hu, hv)]

@@ -70,8 +70,8 @@ def _cfg(**kw):
 
 
 @pytest.mark.parametrize("bad", [
-    {"gc": 1}, {"nx": 1}, {"real_bytes": 2}, {"stepper": 7}, {"bc": 2}, {"reconstruction": 0}, {"friction": 9},
-    {"abi_version": 99}, {"cfl": 0.0}, {"bottom_constant": 1.0},
+    {"gc": 1}, {"nx": 1}, {"real_bytes": 2}, {"stepper": 7}, {"bc": 3}, {"reconstruction": 0}, {"friction": 9},
+    {"abi_version": 99}, {"cfl": 0.0}, {"bottom_constant": 1.0}, {"desingularizing_kappa": 0.0},
 ])
 def test_create_rejects_invalid_configurations_without_touching_the_gpu(lib, bad):
     h = ctypes.c_void_p()
@@ -88,6 +88,6 @@ def test_nonzero_constant_bottom_needs_bottom_source(lib):
 
 
 def test_null_handles_are_rejected(lib):
-    assert lib.vf_step(None, 1.0, None) == N.VF_EINVAL
+    assert lib.vf_step(None, 1.0, 0.0, None) == N.VF_EINVAL
     assert lib.vf_water_volume(None, None) == N.VF_EINVAL
     assert lib.vf_launch_count(None) == 0

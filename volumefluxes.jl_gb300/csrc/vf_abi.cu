@@ -44,6 +44,9 @@ struct vf_handle {
   vf::StepRecord* rec_h = nullptr;
   double* partial = nullptr;
   double* vol_out = nullptr;
+  void* src_field[VF_MAX_SOURCES] = {};   // per-cell source arrays (state layout)
+  double* src_tab[VF_MAX_SOURCES] = {};   // breakpoints then rates/3600
+  int src_tab_n[VF_MAX_SOURCES] = {};
   int vol_blocks = 0;
   vf::StepArgs<double> ad;
   vf::StepArgs<float> af;
@@ -87,6 +90,7 @@ void fill_geom(const vf_handle* h, vf::Geom<T>& g) {
   g.dy = (h->cfg.extent[3] - h->cfg.extent[2]) / h->cfg.ny;
   // Simulator.cfl is stored in the backend's real type (src/simulator.jl:68).
   g.cfl = (double)(T)h->cfg.cfl;
+  g.bc = h->cfg.bc;
 }
 
 template <typename T>
@@ -112,16 +116,64 @@ void fill_phys(const vf_handle* h, vf::Phys<T>& p) {
   p.friction = c.friction;
   p.n_bottom = 0;
   p.n_point = 0;
-  for (int i = 0; i < 8; ++i) p.point_add[i] = (T)0;
+  p.rec_none = c.reconstruction == VF_REC_NONE ? 1 : 0;
+  p.any_dynamic = 0;
+  for (int i = 0; i < 8; ++i) {
+    p.point_add[i] = (T)0;
+    p.point_kind[i] = vf::kConstant;
+    p.point_field[i] = nullptr;
+    p.tab_t[i] = p.tab_r[i] = nullptr;
+    p.tab_n[i] = 0;
+    p.horton[i][0] = p.horton[i][1] = p.horton[i][2] = 0.0;
+  }
   for (int i = 0; i < c.n_sources; ++i) {
-    if (c.source_kind[i] == VF_SRC_BOTTOM) {
+    const int k = c.source_kind[i];
+    if (k == VF_SRC_BOTTOM) {
       ++p.n_bottom;
-    } else if (c.source_kind[i] == VF_SRC_CONST_RAIN) {
-      p.point_add[p.n_point++] = (T)(c.source_rate[i] / 3600);  // compute_rain, source_term_rain.jl:30
-    } else if (c.source_kind[i] == VF_SRC_CONST_INFIL) {
-      p.point_add[p.n_point++] = (T)(-c.source_rate[i]);        // x - r == x + (-r) exactly
+      continue;
+    }
+    const int n = p.n_point++;
+    if (k == VF_SRC_CONST_RAIN) {
+      p.point_add[n] = (T)(c.source_rate[i] / 3600);  // compute_rain, source_term_rain.jl:30
+    } else if (k == VF_SRC_CONST_INFIL) {
+      p.point_add[n] = (T)(-c.source_rate[i]);        // x - r == x + (-r) exactly
+    } else if (k == VF_SRC_TIME_RAIN) {
+      p.point_kind[n] = vf::kTable;
+      p.tab_n[n] = h->src_tab_n[i];
+      p.tab_t[n] = h->src_tab[i];
+      p.tab_r[n] = h->src_tab[i] ? h->src_tab[i] + h->src_tab_n[i] : nullptr;
+      p.any_dynamic = 1;
+    } else if (k == VF_SRC_HORTON) {
+      p.point_kind[n] = vf::kHorton;
+      p.point_field[n] = static_cast<const T*>(h->src_field[i]);
+      p.horton[n][0] = c.source_rate[i];
+      p.horton[n][1] = c.source_aux[i][0];
+      p.horton[n][2] = c.source_aux[i][1];
+      p.any_dynamic = 1;
+    } else if (k == VF_SRC_RAIN_FIELD) {
+      p.point_kind[n] = vf::kField;
+      p.point_field[n] = static_cast<const T*>(h->src_field[i]);
+      p.any_dynamic = 1;
     }
   }
+}
+
+// Column marching covers wall BCs, linear reconstruction and constant sources;
+// everything else runs on the tile kernels.
+void select_variants(vf_handle* h) {
+  const bool march_ok = h->cfg.bc == VF_BC_WALL && h->ad.p.rec_none == 0 && h->ad.p.any_dynamic == 0;
+  h->ad.variant = 1;
+  h->af.variant = march_ok ? 0 : 1;
+  if (const char* kv = std::getenv("VF_KERNELS")) {
+    if (std::strcmp(kv, "tile") == 0) h->ad.variant = h->af.variant = 1;
+    if (std::strcmp(kv, "march") == 0 && march_ok) h->ad.variant = h->af.variant = 0;
+  }
+}
+
+void refresh_params(vf_handle* h) {
+  fill_phys(h, h->ad.p);
+  fill_phys(h, h->af.p);
+  select_variants(h);
 }
 
 int validate(const vf_config* c) {
@@ -134,18 +186,21 @@ int validate(const vf_config* c) {
   if (!(c->extent[1] > c->extent[0]) || !(c->extent[3] > c->extent[2]))
     return fail(nullptr, VF_EINVAL, "extent must be increasing");
   if (c->real_bytes != 8 && c->real_bytes != 4) return fail(nullptr, VF_EINVAL, "real_bytes must be 8 or 4");
-  if (c->reconstruction != VF_REC_LINEAR) return fail(nullptr, VF_EINVAL, "only LinearReconstruction is supported");
+  if (c->reconstruction != VF_REC_LINEAR && c->reconstruction != VF_REC_NONE)
+    return fail(nullptr, VF_EINVAL, "reconstruction must be LinearReconstruction or NoReconstruction");
   if (c->stepper != VF_STEPPER_FE && c->stepper != VF_STEPPER_RK2)
     return fail(nullptr, VF_EINVAL, "stepper must be ForwardEuler or RungeKutta2");
-  if (c->bc != VF_BC_WALL) return fail(nullptr, VF_EINVAL, "only WallBC is supported");
+  if (c->bc != VF_BC_WALL && c->bc != VF_BC_PERIODIC)
+    return fail(nullptr, VF_EINVAL, "boundary must be WallBC or PeriodicBC");
+  if (!(c->desingularizing_kappa > 0) || !(c->depth_cutoff >= 0))
+    return fail(nullptr, VF_EINVAL, "desingularizing_kappa must be positive and depth_cutoff non-negative");
   if (c->friction < VF_FRICTION_NONE || c->friction > VF_FRICTION_BH2021)
     return fail(nullptr, VF_EINVAL, "unknown friction law");
   if (c->n_sources < 0 || c->n_sources > VF_MAX_SOURCES) return fail(nullptr, VF_EINVAL, "too many source terms");
   bool has_bottom_source = false;
   for (int i = 0; i < c->n_sources; ++i) {
     const int k = c->source_kind[i];
-    if (k != VF_SRC_BOTTOM && k != VF_SRC_CONST_RAIN && k != VF_SRC_CONST_INFIL)
-      return fail(nullptr, VF_EINVAL, "unknown source term");
+    if (k < VF_SRC_BOTTOM || k > VF_SRC_RAIN_FIELD) return fail(nullptr, VF_EINVAL, "unknown source term");
     if (k == VF_SRC_BOTTOM) has_bottom_source = true;
   }
   // is_compatible, src/equations/equation.jl:74-84.
@@ -220,6 +275,12 @@ int ensure_ready(vf_handle* h) {
   if (!h) return VF_EINVAL;
   if (!h->have_state) return fail(h, VF_ESTATE, "no state uploaded (call vf_set_interior_state first)");
   if (!h->cfg.bottom_is_constant && !h->have_bottom) return fail(h, VF_ESTATE, "bottom topography not uploaded");
+  for (int i = 0; i < h->cfg.n_sources; ++i) {
+    const int k = h->cfg.source_kind[i];
+    if (k == VF_SRC_TIME_RAIN && !h->src_tab[i]) return fail(h, VF_ESTATE, "TimeDependentRain table not uploaded");
+    if ((k == VF_SRC_HORTON || k == VF_SRC_RAIN_FIELD) && !h->src_field[i])
+      return fail(h, VF_ESTATE, "source field not uploaded");
+  }
   VF_CK(h, cudaSetDevice(h->device));
   return VF_OK;
 }
@@ -236,6 +297,10 @@ void destroy(vf_handle* h) {
   cudaFree(h->rec);
   cudaFree(h->partial);
   cudaFree(h->vol_out);
+  for (int i = 0; i < VF_MAX_SOURCES; ++i) {
+    cudaFree(h->src_field[i]);
+    cudaFree(h->src_tab[i]);
+  }
   if (h->rec_h) cudaFreeHost(h->rec_h);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -303,19 +368,12 @@ int vf_create(const vf_config* cfg, vf_handle** out) {
     return cuda_fail(nullptr, le, "device initialisation");
   }
   fill_geom(h, h->ad.g);
-  fill_phys(h, h->ad.p);
   fill_geom(h, h->af.g);
-  fill_phys(h, h->af.p);
+  refresh_params(h);
   h->ad.rk2 = h->af.rk2 = cfg->stepper == VF_STEPPER_RK2;
   // Default kernels per precision: shared-memory tiles for Float64 (full warps on the
-  // 1/64-rate FP64 pipe), column marching for Float32 (fewest instructions per cell).
-  // VF_KERNELS=tile|march overrides.
-  h->ad.variant = 1;
-  h->af.variant = 0;
-  if (const char* kv = std::getenv("VF_KERNELS")) {
-    if (std::strcmp(kv, "tile") == 0) h->ad.variant = h->af.variant = 1;
-    if (std::strcmp(kv, "march") == 0) h->ad.variant = h->af.variant = 0;
-  }
+  // 1/64-rate FP64 pipe), column marching for Float32 (fewest instructions per cell)
+  // where it applies; VF_KERNELS=tile|march overrides (select_variants).
   h->ad.B = static_cast<const double*>(h->B);
   h->ad.L = static_cast<double*>(h->L);
   h->ad.S = static_cast<double*>(h->S);
@@ -352,6 +410,50 @@ int vf_upload_bottom(vf_handle* h, const void* B_corners) {
                              cudaMemcpyHostToDevice, h->stream));
   VF_CK(h, cudaStreamSynchronize(h->stream));
   h->have_bottom = true;
+  return VF_OK;
+}
+
+int vf_set_source_table(vf_handle* h, int32_t index, const double* times, const double* rates, int32_t n) {
+  if (!h || !times || !rates || n < 1) return fail(h, VF_EINVAL, "invalid table");
+  if (index < 0 || index >= h->cfg.n_sources || h->cfg.source_kind[index] != VF_SRC_TIME_RAIN)
+    return fail(h, VF_EINVAL, "source index is not a TimeDependentRain");
+  VF_CK(h, cudaSetDevice(h->device));
+  double* host = new (std::nothrow) double[2 * n];
+  if (!host) return fail(h, VF_ENOMEM, "host allocation failed");
+  for (int i = 0; i < n; ++i) {
+    host[i] = times[i];
+    host[n + i] = rates[i] / 3600;  // compute_rain, src/sourceterms/source_term_rain.jl:53
+  }
+  if (h->src_tab[index] && h->src_tab_n[index] != n) {
+    cudaFree(h->src_tab[index]);
+    h->src_tab[index] = nullptr;
+  }
+  cudaError_t e = cudaSuccess;
+  if (!h->src_tab[index]) e = cudaMalloc(&h->src_tab[index], sizeof(double) * 2 * n);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->src_tab[index], host, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  delete[] host;
+  if (e != cudaSuccess) return cuda_fail(h, e, "source table upload");
+  h->src_tab_n[index] = n;
+  refresh_params(h);
+  return VF_OK;
+}
+
+int vf_set_source_field(vf_handle* h, int32_t index, const void* field) {
+  if (!h || !field) return fail(h, VF_EINVAL, "NULL argument");
+  if (index < 0 || index >= h->cfg.n_sources ||
+      (h->cfg.source_kind[index] != VF_SRC_HORTON && h->cfg.source_kind[index] != VF_SRC_RAIN_FIELD))
+    return fail(h, VF_EINVAL, "source index is not a HortonInfiltration or rain field");
+  VF_CK(h, cudaSetDevice(h->device));
+  if (!h->src_field[index]) {
+    VF_CK(h, cudaMalloc(&h->src_field[index], (size_t)h->PS * h->elem));
+    VF_CK(h, cudaMemsetAsync(h->src_field[index], 0, (size_t)h->PS * h->elem, h->stream));
+  }
+  int rc = copy_planes(h, h->src_field[index], field, nullptr, 0, 0, h->N1, h->N2, 1, nullptr, nullptr);
+  if (rc) return rc;
+  VF_CK(h, cudaStreamSynchronize(h->stream));
+  refresh_params(h);
   return VF_OK;
 }
 
@@ -399,11 +501,12 @@ int vf_get_interior_state(vf_handle* h, void* w, void* hu, void* hv) {
   return VF_OK;
 }
 
-int vf_step(vf_handle* h, double max_dt, double* dt_out) {
+int vf_step(vf_handle* h, double max_dt, double t, double* dt_out) {
   int rc = ensure_ready(h);
   if (rc) return rc;
   reset_record(h);
   h->rec_h->active[0] = 1;
+  h->rec_h->t[0] = t;
   h->rec_h->explicit_mode = 1;
   h->rec_h->explicit_max_dt = max_dt;
   if ((rc = push_record(h))) return rc;

@@ -33,6 +33,9 @@ constexpr int BHY = TY + 5;
 constexpr int LRN = (TX + 2) * TY > TX * (TY + 2) ? (TX + 2) * TY : TX * (TY + 2);
 constexpr int FN = (TX + 1) * TY > TX * (TY + 1) ? (TX + 1) * TY : TX * (TY + 1);
 constexpr int XOFF = 2;  // leading pad columns in device rows
+#ifndef VF_TILE_MIN_BLOCKS
+#define VF_TILE_MIN_BLOCKS 1
+#endif
 
 // Device-resident step record. Slots indexed by step parity let every kernel
 // of step n read slot n&1 while the stage pass prepares slot (n+1)&1.
@@ -59,7 +62,15 @@ struct Geom {
   int bottom_const;
   T bconst;
   double dx, dy, cfl;
+  int bc;  // 1 wall (src/bc.jl:81-110), 2 periodic (src/bc.jl:29-40)
 };
+
+// Interior source cell of ghost coordinate v (0 <= v < n + 2gc) along one axis:
+// the mirror for walls, the opposite side for periodic boundaries.
+__device__ __forceinline__ int bc_source(int v, int gc, int n, int bc) {
+  if (bc == 2) return v < gc ? v + n : v - n;
+  return v < gc ? 2 * gc - 1 - v : 2 * (gc + n) - 1 - v;
+}
 
 template <typename T>
 __device__ __forceinline__ long long sidx(const Geom<T>& g, int x, int y) {
@@ -102,6 +113,35 @@ __device__ __forceinline__ void load_corners(const Geom<T>& g, const T* __restri
   }
 }
 
+// NoReconstruction for practical SWE, src/reconstruction/noreconstruction.jl:30-46:
+// both face values are (w - B_cell, hu, hv).
+template <typename T>
+__device__ __forceinline__ void no_reconstruction(const T c[3], T Bc, T L[3], T R[3]) {
+  L[0] = R[0] = c[0] - Bc;
+  L[1] = R[1] = c[1];
+  L[2] = R[2] = c[2];
+}
+
+// Stage-1 result U1 of one interior cell read straight from global memory
+// (used for ghost cells, whose source may lie outside the tile).
+template <typename T>
+__device__ __forceinline__ void stage1_point(const Phys<T>& p, T tdt, T u0, T u1, T u2, T l0, T l1, T l2, T S, T Bc,
+                                             T& w, T& hu, T& hv);
+template <typename T>
+__device__ __forceinline__ void u1_global(const Geom<T>& g, const Phys<T>& p, T tdt, const T* __restrict__ U0,
+                                          const T* __restrict__ Lin, const T* __restrict__ Sin,
+                                          const T* __restrict__ B, int x, int y, T& w, T& hu, T& hv) {
+  const long long o = sidx(g, x, y);
+  T Bc = g.bconst;
+  if (!g.bottom_const) {
+    const long long b = (long long)y * g.PB + x + XOFF;
+    Bc = (T)0.25 * (((B[b] + B[b + 1]) + B[b + g.PB]) + B[b + g.PB + 1]);
+  }
+  const T S = p.friction ? Sin[o] : (T)0;
+  stage1_point<T>(p, tdt, U0[o], U0[g.PS + o], U0[2 * g.PS + o], Lin[o], Lin[g.PS + o], Lin[2 * g.PS + o], S, Bc, w,
+                  hu, hv);
+}
+
 // Time derivative of one stage on the tile held in sU (3 planes of HY x HX).
 // acc[k][*] receives -(1/Δx)(F_r-F_l) [+ bottom x], then -(1/Δy)(G_r-G_l)
 // [+ bottom y] for the cells this thread owns (cell tid + k*NT, x fastest).
@@ -122,7 +162,11 @@ __device__ __forceinline__ void tile_derivative(const Phys<T>& p, const T* sU, c
       m[k] = sU[k * HX * HY + c];
       r[k] = sU[k * HX * HY + c + 1];
     }
-    reconstruct_cell<T>(p, l, m, r, bt.template face_l<0>(lx, ly), bt.template face_r<0>(lx, ly), L, R);
+    if (p.rec_none) {
+      no_reconstruction<T>(m, bt.cell(lx, ly), L, R);
+    } else {
+      reconstruct_cell<T>(p, l, m, r, bt.template face_l<0>(lx, ly), bt.template face_r<0>(lx, ly), L, R);
+    }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       sL[k * LRN + idx] = L[k];
@@ -169,7 +213,11 @@ __device__ __forceinline__ void tile_derivative(const Phys<T>& p, const T* sU, c
       m[k] = sU[k * HX * HY + c];
       r[k] = sU[k * HX * HY + c + HX];
     }
-    reconstruct_cell<T>(p, l, m, r, bt.template face_l<1>(lx, ly), bt.template face_r<1>(lx, ly), L, R);
+    if (p.rec_none) {
+      no_reconstruction<T>(m, bt.cell(lx, ly), L, R);
+    } else {
+      reconstruct_cell<T>(p, l, m, r, bt.template face_l<1>(lx, ly), bt.template face_r<1>(lx, ly), L, R);
+    }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       sL[k * LRN + idx] = L[k];
@@ -237,10 +285,11 @@ struct SmemFlux {
   T R[3 * LRN];
   T F[3 * FN];
   unsigned long long red[2][NT / 32];
+  T scal[8];
 };
 
 template <typename T>
-__global__ void __launch_bounds__(NT) k_flux(Geom<T> g, Phys<T> p, const T* __restrict__ U, const T* __restrict__ B,
+__global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_flux(Geom<T> g, Phys<T> p, const T* __restrict__ U, const T* __restrict__ B,
                                              T* __restrict__ Lout, T* __restrict__ Sout, StepRecord* rec, int parity) {
   if (!rec->active[parity]) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -258,6 +307,7 @@ __global__ void __launch_bounds__(NT) k_flux(Geom<T> g, Phys<T> p, const T* __re
     for (int k = 0; k < 3; ++k) s.U[k * HX * HY + idx] = ok ? U[k * g.PS + o] : (T)0;
   }
   if (!g.bottom_const) load_corners(g, B, s.B, x0, y0);
+  if (p.any_dynamic && tid == 0) point_scalars<T>(p, rec->t[parity], s.scal);
   __syncthreads();
 
   BTile<T> bt{s.B, g.bottom_const, g.bconst};
@@ -270,8 +320,8 @@ __global__ void __launch_bounds__(NT) k_flux(Geom<T> g, Phys<T> p, const T* __re
     const int c = tid + k * NT;
     const int lx = c % TX, ly = c / TX;
     if (lx >= nvx || ly >= nvy) continue;
-    acc[k][0] = add_point_sources<T>(p, acc[k][0]);
     const long long o = sidx(g, x0 + lx, y0 + ly);
+    acc[k][0] = p.any_dynamic ? add_point_sources<T>(p, acc[k][0], s.scal, o) : add_point_sources<T>(p, acc[k][0]);
 #pragma unroll
     for (int j = 0; j < 3; ++j) Lout[j * g.PS + o] = acc[k][j];
     if (p.friction) {
@@ -335,8 +385,9 @@ __device__ __forceinline__ void carry_record(StepRecord* rec, int parity) {
   rec->active[parity ^ 1] = 0;
 }
 
-// Wall ghosts written by the owner of each mirror source, src/bc.jl:81-110.
-// X ghosts (interior rows) get hu negated, Y ghosts (interior columns) hv.
+// Ghosts written by the owner of each boundary source cell: wall mirrors
+// (src/bc.jl:81-110; x ghosts negate hu, y ghosts hv) or periodic copies
+// (src/bc.jl:29-40). Corner ghosts are never written, as in the reference.
 template <typename T>
 __device__ __forceinline__ void store_with_ghosts(const Geom<T>& g, T* __restrict__ Uo, int gx, int gy, T w, T hu,
                                                   T hv) {
@@ -344,34 +395,41 @@ __device__ __forceinline__ void store_with_ghosts(const Geom<T>& g, T* __restric
   Uo[o] = w;
   Uo[g.PS + o] = hu;
   Uo[2 * g.PS + o] = hv;
-  const int lo = g.gc, hi = g.gc + g.nx - 1;
-  int gxs[2] = {-1, -1};
-  if (gx == lo) gxs[0] = lo - 1;
-  if (gx == lo + 1) gxs[0] = lo - 2;
-  if (gx == hi) gxs[1] = hi + 1;
-  if (gx == hi - 1) gxs[1] = hi + 2;
+  int gxs[2] = {-1, -1}, gys[2] = {-1, -1};
+  const T sx = g.bc == 2 ? (T)1 : (T)-1;  // momentum sign across an x ghost
+  if (g.bc == 2) {
+    if (gx < 2 * g.gc) gxs[0] = gx + g.nx;
+    if (gx >= g.nx) gxs[1] = gx - g.nx;
+    if (gy < 2 * g.gc) gys[0] = gy + g.ny;
+    if (gy >= g.ny) gys[1] = gy - g.ny;
+  } else {
+    const int lo = g.gc, hi = g.gc + g.nx - 1;
+    if (gx == lo) gxs[0] = lo - 1;
+    if (gx == lo + 1) gxs[0] = lo - 2;
+    if (gx == hi) gxs[1] = hi + 1;
+    if (gx == hi - 1) gxs[1] = hi + 2;
+    const int ylo = g.gc, yhi = g.gc + g.ny - 1;
+    if (gy == ylo) gys[0] = ylo - 1;
+    if (gy == ylo + 1) gys[0] = ylo - 2;
+    if (gy == yhi) gys[1] = yhi + 1;
+    if (gy == yhi - 1) gys[1] = yhi + 2;
+  }
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
     if (gxs[i] >= 0) {
       const long long q = sidx(g, gxs[i], gy);
       Uo[q] = w;
-      Uo[g.PS + q] = -hu;
+      Uo[g.PS + q] = sx * hu;
       Uo[2 * g.PS + q] = hv;
     }
   }
-  const int ylo = g.gc, yhi = g.gc + g.ny - 1;
-  int gys[2] = {-1, -1};
-  if (gy == ylo) gys[0] = ylo - 1;
-  if (gy == ylo + 1) gys[0] = ylo - 2;
-  if (gy == yhi) gys[1] = yhi + 1;
-  if (gy == yhi - 1) gys[1] = yhi + 2;
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
     if (gys[i] >= 0) {
       const long long q = sidx(g, gx, gys[i]);
       Uo[q] = w;
       Uo[g.PS + q] = hu;
-      Uo[2 * g.PS + q] = -hv;
+      Uo[2 * g.PS + q] = sx * hv;
     }
   }
 }
@@ -400,10 +458,11 @@ struct SmemStage {
   T R[3 * LRN];
   T F[3 * FN];
   double dt;
+  T scal[8];
 };
 
 template <typename T>
-__global__ void __launch_bounds__(NT) k_stage2(Geom<T> g, Phys<T> p, const T* __restrict__ U0, const T* __restrict__ B,
+__global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_stage2(Geom<T> g, Phys<T> p, const T* __restrict__ U0, const T* __restrict__ B,
                                                const T* __restrict__ Lin, const T* __restrict__ Sin, T* __restrict__ Uo,
                                                StepRecord* rec, int parity) {
   const bool root = blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0;
@@ -418,19 +477,23 @@ __global__ void __launch_bounds__(NT) k_stage2(Geom<T> g, Phys<T> p, const T* __
   const int nvx = min(TX, g.gc + g.nx - x0), nvy = min(TY, g.gc + g.ny - y0);
 
   if (tid == 0) s.dt = step_dt<T>(g, rec, parity);
+  if (p.any_dynamic && tid == 1) point_scalars<T>(p, rec->t[parity], s.scal);
   if (!g.bottom_const) load_corners(g, B, s.B, x0, y0);
   __syncthreads();
   const double dt = s.dt;
   const T tdt = (T)dt;
   BTile<T> bt{s.B, g.bottom_const, g.bconst};
 
-  // U1 on the interior cells of tile + halo, from U0, L, S.
+  // U1 on tile + halo, from U0, L, S. Ghost cells take U1 of their boundary
+  // source cell (src/bc.jl:29-40, 81-110), computed the same pointwise way;
+  // corner ghosts are never read and stay zero.
   for (int idx = tid; idx < HX * HY; idx += NT) {
     const int lx = idx % HX - 2, ly = idx / HX - 2;
     const int gx = x0 + lx, gy = y0 + ly;
-    const bool inside = gx >= g.gc && gx < g.gc + g.nx && gy >= g.gc && gy < g.gc + g.ny;
+    const bool xin = gx >= g.gc && gx < g.gc + g.nx;
+    const bool yin = gy >= g.gc && gy < g.gc + g.ny;
     T w = (T)0, hu = (T)0, hv = (T)0;
-    if (inside) {
+    if (xin && yin) {
       const long long o = sidx(g, gx, gy);
       const T a0 = U0[o], a1 = U0[g.PS + o], a2 = U0[2 * g.PS + o];
       const T S = p.friction ? Sin[o] : (T)0;
@@ -441,31 +504,16 @@ __global__ void __launch_bounds__(NT) k_stage2(Geom<T> g, Phys<T> p, const T* __
         s.U0[TX * TY + t] = a1;
         s.U0[2 * TX * TY + t] = a2;
       }
+    } else if (yin && gx < g.N1) {
+      u1_global<T>(g, p, tdt, U0, Lin, Sin, B, bc_source(gx, g.gc, g.nx, g.bc), gy, w, hu, hv);
+      if (g.bc != 2) hu = -hu;
+    } else if (xin && gy < g.N2) {
+      u1_global<T>(g, p, tdt, U0, Lin, Sin, B, gx, bc_source(gy, g.gc, g.ny, g.bc), w, hu, hv);
+      if (g.bc != 2) hv = -hv;
     }
     s.U1[idx] = w;
     s.U1[HX * HY + idx] = hu;
     s.U1[2 * HX * HY + idx] = hv;
-  }
-  __syncthreads();
-  // Wall ghosts of U1 inside the halo (src/bc.jl:81-110); corner ghosts are never read.
-  for (int idx = tid; idx < HX * HY; idx += NT) {
-    const int lx = idx % HX - 2, ly = idx / HX - 2;
-    const int gx = x0 + lx, gy = y0 + ly;
-    const bool xin = gx >= g.gc && gx < g.gc + g.nx;
-    const bool yin = gy >= g.gc && gy < g.gc + g.ny;
-    if (yin && !xin && gx < g.N1) {
-      const int sx = gx < g.gc ? 2 * g.gc - 1 - gx : 2 * (g.gc + g.nx) - 1 - gx;
-      const int si = (ly + 2) * HX + (sx - x0 + 2);
-      s.U1[idx] = s.U1[si];
-      s.U1[HX * HY + idx] = -s.U1[HX * HY + si];
-      s.U1[2 * HX * HY + idx] = s.U1[2 * HX * HY + si];
-    } else if (xin && !yin && gy < g.N2) {
-      const int sy = gy < g.gc ? 2 * g.gc - 1 - gy : 2 * (g.gc + g.ny) - 1 - gy;
-      const int si = (sy - y0 + 2) * HX + (lx + 2);
-      s.U1[idx] = s.U1[si];
-      s.U1[HX * HY + idx] = s.U1[HX * HY + si];
-      s.U1[2 * HX * HY + idx] = -s.U1[2 * HX * HY + si];
-    }
   }
   __syncthreads();
 
@@ -478,7 +526,8 @@ __global__ void __launch_bounds__(NT) k_stage2(Geom<T> g, Phys<T> p, const T* __
     const int c = tid + k * NT;
     const int lx = c % TX, ly = c / TX;
     if (lx >= nvx || ly >= nvy) continue;
-    acc[k][0] = add_point_sources<T>(p, acc[k][0]);
+    const long long o = sidx(g, x0 + lx, y0 + ly);
+    acc[k][0] = p.any_dynamic ? add_point_sources<T>(p, acc[k][0], s.scal, o) : add_point_sources<T>(p, acc[k][0]);
     const int ci = (ly + 2) * HX + lx + 2;
     const T v0 = s.U1[ci], v1 = s.U1[HX * HY + ci], v2 = s.U1[2 * HX * HY + ci];
     T w = v0 + tdt * acc[k][0];
@@ -488,12 +537,7 @@ __global__ void __launch_bounds__(NT) k_stage2(Geom<T> g, Phys<T> p, const T* __
     hu = (T)0.5 * (s.U0[TX * TY + c] + hu);
     hv = (T)0.5 * (s.U0[2 * TX * TY + c] + hv);
     const T Bc = bt.cell(lx, ly);
-    if (p.friction) {
-      const T S = friction_factor<T>(p, v0, v1, v2, Bc);
-      const T den = (T)1 - tdt * S;
-      hu = vdiv<T>(hu, den);
-      hv = vdiv<T>(hv, den);
-    }
+    if (p.friction && friction_active<T>(v1, v2)) apply_friction<T>(tdt, friction_factor<T>(p, v0, v1, v2, Bc), hu, hv);
     dry_clamp<T>(p, w, hu, hv, Bc);
     store_with_ghosts<T>(g, Uo, x0 + lx, y0 + ly, w, hu, hv);
   }
@@ -536,29 +580,32 @@ __global__ void __launch_bounds__(NT) k_apply_fe(Geom<T> g, Phys<T> p, const T* 
   if (root) advance_record<T>(rec, parity, dt);
 }
 
-// Wall boundary update of a whole volume, src/bc.jl:81-110 (used after uploads).
+// Boundary update of a whole volume (after uploads): wall, src/bc.jl:81-110,
+// or periodic, src/bc.jl:29-40. Ghost columns at interior rows, ghost rows at
+// interior columns; corners untouched.
 template <typename T>
-__global__ void k_bc_wall(Geom<T> g, T* __restrict__ U) {
-  const int n_x = g.ny * 2 * g.gc;  // x ghosts at interior rows
+__global__ void k_bc(Geom<T> g, T* __restrict__ U) {
+  const int n_x = g.ny * 2 * g.gc;
   const int n_y = g.nx * 2 * g.gc;
+  const T sgn = g.bc == 2 ? (T)1 : (T)-1;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_x + n_y; idx += gridDim.x * blockDim.x) {
     if (idx < n_x) {
       const int j = g.gc + idx / (2 * g.gc), r = idx % (2 * g.gc);
       const int gx = r < g.gc ? r : g.gc + g.nx + (r - g.gc);
-      const int sx = gx < g.gc ? 2 * g.gc - 1 - gx : 2 * (g.gc + g.nx) - 1 - gx;
+      const int sx = bc_source(gx, g.gc, g.nx, g.bc);
       const long long d = sidx(g, gx, j), sI = sidx(g, sx, j);
       U[d] = U[sI];
-      U[g.PS + d] = -U[g.PS + sI];
+      U[g.PS + d] = sgn * U[g.PS + sI];
       U[2 * g.PS + d] = U[2 * g.PS + sI];
     } else {
       const int q = idx - n_x;
       const int i = g.gc + q / (2 * g.gc), r = q % (2 * g.gc);
       const int gy = r < g.gc ? r : g.gc + g.ny + (r - g.gc);
-      const int sy = gy < g.gc ? 2 * g.gc - 1 - gy : 2 * (g.gc + g.ny) - 1 - gy;
+      const int sy = bc_source(gy, g.gc, g.ny, g.bc);
       const long long d = sidx(g, i, gy), sI = sidx(g, i, sy);
       U[d] = U[sI];
       U[g.PS + d] = U[g.PS + sI];
-      U[2 * g.PS + d] = -U[2 * g.PS + sI];
+      U[2 * g.PS + d] = sgn * U[2 * g.PS + sI];
     }
   }
 }

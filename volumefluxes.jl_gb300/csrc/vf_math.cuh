@@ -16,6 +16,13 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "vf_idiv.cuh"
+
+// Float64 division on the integer pipe (1) or the FP64 pipe (0).
+#ifndef VF_FP64_INT_DIV
+#define VF_FP64_INT_DIV 1
+#endif
+
 namespace vf {
 
 // ---------------------------------------------------------------------------
@@ -52,7 +59,16 @@ struct Arith<double> {
   // Julia's max/min: -0.0 < +0.0.
   static __device__ __forceinline__ double max(double x, double y) { return key(x) > key(y) ? x : y; }
   static __device__ __forceinline__ double min(double x, double y) { return key(x) < key(y) ? x : y; }
-  static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+  // Correctly rounded division on the integer pipe (vf_idiv.cuh); the FP64
+  // pipe's division only for operands or results outside the normal range.
+  static __device__ __forceinline__ double div(double a, double b) {
+#if VF_FP64_INT_DIV
+    double q;
+    return idiv_normal(a, b, &q) ? q : a / b;
+#else
+    return a / b;
+#endif
+  }
   static __device__ __forceinline__ double rcp(double b) { return 1.0 / b; }
   static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
 };
@@ -161,8 +177,67 @@ struct Phys {
   int friction;               // VF_FRICTION_*
   int n_bottom;               // SourceTermBottom entries
   int n_point;                // rain/infiltration entries, applied in order
-  T point_add[8];             // +rate/3600 for rain, -rate for infiltration
+  int rec_none;               // NoReconstruction instead of LinearReconstruction
+  int any_dynamic;            // some point source is not a constant
+  int point_kind[8];          // PointKind
+  T point_add[8];             // kConstant: +rate/3600 for rain, -rate for infiltration
+  const T* point_field[8];    // kHorton: factor, kField: rain rate [m/s]; total grid, state layout
+  const double* tab_t[8];     // kTable: breakpoints of TimeDependentRain
+  const double* tab_r[8];     // kTable: rates/3600 per breakpoint
+  int tab_n[8];
+  double horton[8][3];        // kHorton: fc, f0, k
 };
+
+enum PointKind { kConstant = 0, kTable = 1, kHorton = 2, kField = 3 };
+
+// Deterministic exp for HortonInfiltration: Cody-Waite reduction by ln 2 (split
+// in two doubles), Taylor polynomial of degree 14 in Horner form with fused
+// multiply-adds, exact scaling by 2^k. The oracle computes the same bits.
+__device__ __forceinline__ double det_exp(double x) {
+  if (x != x) return x;
+  if (x > 709.782712893384) return __longlong_as_double(0x7ff0000000000000ll);
+  if (x < -745.1332191019412) return 0.0;
+  const double inv_ln2 = 0x1.71547652b82fep+0;
+  const double ln2_hi = 0x1.62e42fefa39efp-1, ln2_lo = 0x1.abc9e3b39803fp-56;
+  double kd = x * inv_ln2;
+  kd = (kd + 6755399441055744.0) - 6755399441055744.0;  // round to nearest integer
+  double r = fma(-kd, ln2_hi, x);
+  r = fma(-kd, ln2_lo, r);
+  const double c[15] = {0x1.0000000000000p+0, 0x1.0000000000000p+0, 0x1.0000000000000p-1,
+                        0x1.5555555555555p-3, 0x1.5555555555555p-5, 0x1.1111111111111p-7,
+                        0x1.6c16c16c16c17p-10, 0x1.a01a01a01a01ap-13, 0x1.a01a01a01a01ap-16,
+                        0x1.71de3a556c734p-19, 0x1.27e4fb7789f5cp-22, 0x1.ae64567f544e4p-26,
+                        0x1.1eed8eff8d898p-29, 0x1.6124613a86d09p-33, 0x1.93974a8c07c9dp-37};
+  double q = c[14];
+#pragma unroll
+  for (int n = 13; n >= 0; --n) q = fma(q, r, c[n]);
+  int k = (int)kd;
+  if (k > 1023) { q = q * 2.0; k -= 1; }
+  if (k < -1022) return (q * __longlong_as_double((long long)(k + 54 + 1023) << 52)) * 0x1p-54;
+  return q * __longlong_as_double((long long)(k + 1023) << 52);
+}
+
+// Per-step scalars of the time-dependent point sources at the step's start
+// time t (the same t for both RK2 stages, src/system.jl:71-73):
+// TimeDependentRain's tabulated rate (src/sourceterms/source_term_rain.jl:45-54)
+// and Horton's fc + (f0 - fc)*exp(-k*t) (src/sourceterms/source_term_infiltration.jl:68-70).
+template <typename T>
+__device__ __forceinline__ void point_scalars(const Phys<T>& p, double t, T* out) {
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    out[n] = (T)0;
+    if (n >= p.n_point) continue;
+    if (p.point_kind[n] == kTable) {
+      int idx = 0;
+      while (idx + 1 < p.tab_n[n] && !(t < p.tab_t[n][idx + 1])) ++idx;
+      out[n] = (T)p.tab_r[n][idx];
+    } else if (p.point_kind[n] == kHorton) {
+      const T fc = (T)p.horton[n][0], f0 = (T)p.horton[n][1], k = (T)p.horton[n][2];
+      const T decay = (T)det_exp((double)(-k * (T)t));
+      out[n] = fc + (f0 - fc) * decay;
+    }
+  }
+}
 
 // ΔB/Δ of the bottom source; exact reciprocal multiply when Δ is a power of two.
 template <typename T>
@@ -171,12 +246,27 @@ __device__ __forceinline__ T slope_over(T dB, T delta, T inv_delta, int pow2) {
 }
 
 // Rain and infiltration in list order (src/system.jl:71-73), unrolled so the
-// parameter block is never indexed dynamically.
+// parameter block is never indexed dynamically. `scal` holds point_scalars();
+// `cell` is the cell's offset in the state layout (for per-cell arrays).
 template <typename T>
 __device__ __forceinline__ T add_point_sources(const Phys<T>& p, T acc0) {
 #pragma unroll
   for (int n = 0; n < 8; ++n)
     if (n < p.n_point) acc0 = acc0 + p.point_add[n];
+  return acc0;
+}
+template <typename T>
+__device__ __forceinline__ T add_point_sources(const Phys<T>& p, T acc0, const T* scal, long long cell) {
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    if (n >= p.n_point) continue;
+    switch (p.point_kind[n]) {
+      case kConstant: acc0 = acc0 + p.point_add[n]; break;
+      case kTable: acc0 = acc0 + scal[n]; break;
+      case kHorton: acc0 = acc0 - p.point_field[n][cell] * scal[n]; break;
+      default: acc0 = acc0 + p.point_field[n][cell]; break;
+    }
+  }
   return acc0;
 }
 

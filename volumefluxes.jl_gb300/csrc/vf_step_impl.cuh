@@ -71,7 +71,7 @@ cudaError_t launch_bc_impl(const Geom<T>& g, T* U, cudaStream_t st) {
   const int n = 2 * g.gc * (g.nx + g.ny);
   int blocks = (n + NT - 1) / NT;
   if (blocks > 4096) blocks = 4096;
-  k_bc_wall<T><<<blocks, NT, 0, st>>>(g, U);
+  k_bc<T><<<blocks, NT, 0, st>>>(g, U);
   return cudaGetLastError();
 }
 

@@ -13,6 +13,7 @@ from .api import (  # noqa: F401
     Reconstruction, LinearReconstruction, NoReconstruction, minmod,
     NumericalFlux, CentralUpwind,
     SourceTerm, SourceTermBottom, SourceTermRain, SourceTermInfiltration, ConstantRain, ConstantInfiltration,
+    TimeDependentRain, FunctionalRain, HortonInfiltration,
     compute_rain, compute_infiltration,
     friction_bsa2012, friction_fcg2016, friction_bh2021, ImplicitFriction,
     TimeStepper, RungeKutta2, ForwardEulerStepper, number_of_substeps,

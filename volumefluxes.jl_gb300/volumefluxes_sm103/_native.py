@@ -11,20 +11,22 @@ from pathlib import Path
 
 import numpy as np
 
-LIB_PATH = Path(__file__).resolve().parent / "lib" / "libvfsm103.so"
+LIB_PATH = Path(os.environ.get("VF_SM103_LIB", Path(__file__).resolve().parent / "lib" / "libvfsm103.so"))
 
-VF_ABI_VERSION = 1
+VF_ABI_VERSION = 2
 VF_MAX_SOURCES = 8
 VF_OK, VF_EINVAL, VF_ENOMEM, VF_ECUDA, VF_ESTATE = 0, -1, -2, -3, -4
 VF_SRC_BOTTOM, VF_SRC_CONST_RAIN, VF_SRC_CONST_INFIL = 1, 2, 3
+VF_SRC_TIME_RAIN, VF_SRC_HORTON, VF_SRC_RAIN_FIELD = 4, 5, 6
 VF_FRICTION_NONE, VF_FRICTION_BSA2012, VF_FRICTION_FCG2016, VF_FRICTION_BH2021 = 0, 1, 2, 3
 VF_STEPPER_FE, VF_STEPPER_RK2 = 1, 2
-VF_BC_WALL = 1
-VF_REC_LINEAR = 1
+VF_BC_WALL, VF_BC_PERIODIC = 1, 2
+VF_REC_LINEAR, VF_REC_NONE = 1, 2
 
 # Every symbol include/volumefluxes_sm103.h declares.
 EXPORTED_SYMBOLS = (
-    "vf_create", "vf_destroy", "vf_upload_bottom", "vf_set_interior_state", "vf_upload_state",
+    "vf_create", "vf_destroy", "vf_upload_bottom", "vf_set_source_table", "vf_set_source_field",
+    "vf_set_interior_state", "vf_upload_state",
     "vf_download_state", "vf_get_interior_state", "vf_step", "vf_simulate", "vf_water_volume",
     "vf_device_state", "vf_stream", "vf_time_steps", "vf_time_kernels", "vf_last_error", "vf_launch_count",
     "vf_water_volume_static",
@@ -44,6 +46,7 @@ class VfConfig(C.Structure):
         ("n_sources", C.c_int32),
         ("source_kind", C.c_int32 * VF_MAX_SOURCES),
         ("source_rate", C.c_double * VF_MAX_SOURCES),
+        ("source_aux", (C.c_double * 2) * VF_MAX_SOURCES),
         ("friction", C.c_int32), ("friction_Cz", C.c_double),
         ("stepper", C.c_int32), ("bc", C.c_int32), ("cfl", C.c_double),
         ("bottom_is_constant", C.c_int32), ("bottom_constant", C.c_double),
@@ -90,7 +93,9 @@ def load(build_if_missing: bool = False):
         "vf_upload_state": (C.c_int, [H, C.c_void_p]),
         "vf_download_state": (C.c_int, [H, C.c_void_p]),
         "vf_get_interior_state": (C.c_int, [H, C.c_void_p, C.c_void_p, C.c_void_p]),
-        "vf_step": (C.c_int, [H, C.c_double, C.POINTER(C.c_double)]),
+        "vf_step": (C.c_int, [H, C.c_double, C.c_double, C.POINTER(C.c_double)]),
+        "vf_set_source_table": (C.c_int, [H, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
+        "vf_set_source_field": (C.c_int, [H, C.c_int32, C.c_void_p]),
         "vf_simulate": (C.c_int, [H, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_double, C.c_int64,
                                   C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
         "vf_water_volume": (C.c_int, [H, C.POINTER(C.c_double)]),

@@ -304,13 +304,74 @@ class ConstantInfiltration(SourceTermInfiltration):
         self.infiltration_rate = float(infiltration_rate)
 
 
-def compute_rain(rain: ConstantRain, *args) -> float:
-    """src/sourceterms/source_term_rain.jl:30."""
+class TimeDependentRain(SourceTermRain):
+    """TimeDependentRain(rain_rates, time=[0.0]) with rates in m/h, src/sourceterms/source_term_rain.jl:32-41."""
+
+    def __init__(self, rain_rates, time=(0.0,)):
+        rates = np.asarray(rain_rates, dtype=np.float64).reshape(-1)
+        times = np.asarray(time, dtype=np.float64).reshape(-1)
+        if rates.shape != times.shape:
+            raise DomainError("Dimensions of input parameters rain_rates and time does not match")
+        self.rain_rates, self.time = rates, times
+
+
+class FunctionalRain(SourceTermRain):
+    """FunctionalRain(rain_function, grid): rain_function(t, x, y) in m/s at cell centres,
+    src/sourceterms/source_term_rain.jl:57-68. The host evaluates it over the grid at the
+    step's start time and uploads the field (the closure cannot cross the C ABI)."""
+
+    def __init__(self, rain_function: Callable, grid: CartesianGrid):
+        self.rain_function = rain_function
+        self.grid = grid
+
+    def field(self, t: float) -> np.ndarray:
+        g = self.grid
+        I = np.arange(1, g.totalcells[0] + 1, dtype=np.float64)
+        J = np.arange(1, g.totalcells[1] + 1, dtype=np.float64)
+        x = g.extent[0, 0] + compute_dx(g) * (I - 0.5 - g.ghostcells[0])
+        y = g.extent[1, 0] + compute_dy(g) * (J - 0.5 - g.ghostcells[1])
+        X, Y = np.meshgrid(x, y, indexing="ij")
+        try:
+            f = np.asarray(self.rain_function(t, X, Y), dtype=np.float64)
+            if f.shape != X.shape:
+                f = np.broadcast_to(f, X.shape)
+        except Exception:
+            f = np.vectorize(lambda a, b: float(self.rain_function(t, a, b)))(X, Y)
+        return np.ascontiguousarray(f, dtype=np.float64)
+
+
+class HortonInfiltration(SourceTermInfiltration):
+    """HortonInfiltration(grid, backend; factor=1.0, fc=3.272e-5, f0=1.977e-4, k=2.43e-3),
+    src/sourceterms/source_term_infiltration.jl:21-47: f(t) = factor*(fc + (f0 - fc)*exp(-k*t))."""
+
+    def __init__(self, grid: CartesianGrid, backend=None, *, factor=1.0, fc: float = 3.272e-5, f0: float = 1.977e-4,
+                 k: float = 2.43e-3):
+        fa = np.asarray(factor, dtype=np.float64)
+        if fa.ndim == 0:
+            fa = np.full(grid.size(), float(fa))
+        elif fa.shape != grid.size():
+            raise DomainError(f"Infiltration factor should be of size {grid.size()} but got {fa.shape}")
+        self.factor, self.fc, self.f0, self.k = fa, float(fc), float(f0), float(k)
+
+
+def compute_rain(rain, t=None, index=None):
+    """src/sourceterms/source_term_rain.jl:30,45-54,65-68 (host evaluation)."""
+    if isinstance(rain, TimeDependentRain):
+        idx = 0
+        while idx + 1 < rain.time.size and not (t < rain.time[idx + 1]):
+            idx += 1
+        return rain.rain_rates[idx] / 3600
+    if isinstance(rain, FunctionalRain):
+        x, y = cell_center(rain.grid, index)
+        return rain.rain_function(t, x, y)
     return rain.rain_rate / 3600
 
 
-def compute_infiltration(infiltration: ConstantInfiltration, *args) -> float:
-    """src/sourceterms/source_term_infiltration.jl:79-81."""
+def compute_infiltration(infiltration, t=None, index=None):
+    """src/sourceterms/source_term_infiltration.jl:68-81 (host evaluation; index is 1-based)."""
+    if isinstance(infiltration, HortonInfiltration):
+        f = infiltration
+        return f.factor[index[0] - 1, index[1] - 1] * (f.fc + (f.f0 - f.fc) * math.exp(-f.k * t))
     return infiltration.infiltration_rate
 
 
@@ -490,18 +551,37 @@ class Simulator:
         if isinstance(eqB, BottomTopography2D):
             B = np.ascontiguousarray(np.asarray(eqB.B, dtype=self.dtype).T)
             N.check(self._lib, self._h, self._lib.vf_upload_bottom(self._h, N.ptr(B)))
+        self._functional = []
+        for i, st in enumerate(system.source_terms):
+            if isinstance(st, TimeDependentRain):
+                t_, r_ = np.ascontiguousarray(st.time), np.ascontiguousarray(st.rain_rates)
+                N.check(self._lib, self._h, self._lib.vf_set_source_table(self._h, i, N.ptr(t_), N.ptr(r_), t_.size))
+            elif isinstance(st, HortonInfiltration):
+                self._upload_field(i, st.factor)
+            elif isinstance(st, FunctionalRain):
+                self._functional.append((i, st))
+
+    def _upload_field(self, index: int, field: np.ndarray):
+        f = np.ascontiguousarray(np.asarray(field, dtype=self.dtype).T)  # x fastest
+        N.check(self._lib, self._h, self._lib.vf_set_source_field(self._h, index, N.ptr(f)))
+
+    def _refresh_functional(self):
+        """Re-evaluate FunctionalRain at the step's start time (src/sourceterms/source_term_rain.jl:65-76)."""
+        for i, st in self._functional:
+            self._upload_field(i, st.field(self.t))
 
     def _config(self) -> N.VfConfig:
         s, g = self.system, self.grid
         eq = s.equation
         if not isinstance(eq, ShallowWaterEquations):
             raise ArgumentError("the sm_103a backend runs ShallowWaterEquations (2D practical SWE) only")
-        if not isinstance(s.reconstruction, LinearReconstruction):
+        if not isinstance(s.reconstruction, (LinearReconstruction, NoReconstruction)):
             raise ArgumentError(f"{type(s.reconstruction).__name__} is not implemented on the sm_103a backend")
         if not isinstance(s.numericalflux, CentralUpwind):
             raise ArgumentError(f"{type(s.numericalflux).__name__} is not implemented on the sm_103a backend")
-        if not isinstance(g.boundary, WallBC):
-            raise ArgumentError(f"{type(g.boundary).__name__} is not implemented on the sm_103a backend (WallBC only)")
+        if not isinstance(g.boundary, (WallBC, PeriodicBC)):
+            raise ArgumentError(f"{type(g.boundary).__name__} is not implemented on the sm_103a backend "
+                                "(WallBC and PeriodicBC are)")
         if g.gc != 2:
             raise ArgumentError("the sm_103a backend needs CartesianGrid(...; gc=2)")
         if isinstance(self.timestepper, RungeKutta2):
@@ -518,8 +598,10 @@ class Simulator:
         cfg.real_bytes = self.dtype.itemsize
         cfg.g, cfg.rho = eq.g, eq.rho
         cfg.depth_cutoff, cfg.desingularizing_kappa = eq.depth_cutoff, eq.desingularizing_kappa
-        cfg.reconstruction = N.VF_REC_LINEAR
-        cfg.theta = s.reconstruction.theta
+        if isinstance(s.reconstruction, NoReconstruction):
+            cfg.reconstruction, cfg.theta = N.VF_REC_NONE, 0.0
+        else:
+            cfg.reconstruction, cfg.theta = N.VF_REC_LINEAR, s.reconstruction.theta
         if len(s.source_terms) > N.VF_MAX_SOURCES:
             raise ArgumentError("too many source terms")
         for i, st in enumerate(s.source_terms):
@@ -529,6 +611,13 @@ class Simulator:
                 cfg.source_kind[i], cfg.source_rate[i] = N.VF_SRC_CONST_RAIN, st.rain_rate
             elif isinstance(st, ConstantInfiltration):
                 cfg.source_kind[i], cfg.source_rate[i] = N.VF_SRC_CONST_INFIL, st.infiltration_rate
+            elif isinstance(st, TimeDependentRain):
+                cfg.source_kind[i] = N.VF_SRC_TIME_RAIN
+            elif isinstance(st, HortonInfiltration):
+                cfg.source_kind[i], cfg.source_rate[i] = N.VF_SRC_HORTON, st.fc
+                cfg.source_aux[i][0], cfg.source_aux[i][1] = st.f0, st.k
+            elif isinstance(st, FunctionalRain):
+                cfg.source_kind[i] = N.VF_SRC_RAIN_FIELD
             else:
                 raise ArgumentError(f"{type(st).__name__} is not implemented on the sm_103a backend")
         cfg.n_sources = len(s.source_terms)
@@ -542,7 +631,7 @@ class Simulator:
         else:
             raise ArgumentError(f"{type(fr).__name__} is not implemented on the sm_103a backend")
         cfg.stepper = stepper
-        cfg.bc = N.VF_BC_WALL
+        cfg.bc = N.VF_BC_PERIODIC if isinstance(g.boundary, PeriodicBC) else N.VF_BC_WALL
         cfg.cfl = self.cfl
         if isinstance(eq.B, ConstantBottomTopography):
             cfg.bottom_is_constant, cfg.bottom_constant = 1, eq.B.B
@@ -629,7 +718,9 @@ def perform_step(simulator: Simulator, max_dt: float) -> None:
     """perform_step!(simulator, max_dt), src/simulator.jl:145-177 (does not advance t)."""
     dt = C.c_double()
     lib = simulator._lib
-    N.check(lib, simulator.handle, lib.vf_step(simulator.handle, float(max_dt), C.byref(dt)))
+    if simulator._functional:
+        simulator._refresh_functional()
+    N.check(lib, simulator.handle, lib.vf_step(simulator.handle, float(max_dt), float(simulator.t), C.byref(dt)))
     simulator.current_timestep = dt.value
 
 
@@ -692,7 +783,7 @@ def simulate_to_time(simulator: Simulator, endtime: float, *, match_endtime: boo
     h = simulator.handle
     max_ts = -1.0 if maximum_timestep is None else float(maximum_timestep)
     writers = None if callback is None else _interval_writers(callback)
-    if callback is None or writers is not None:
+    if (callback is None or writers is not None) and not simulator._functional:
         while simulator.t < endtime:
             stop = min((w.current_t for w in writers), default=math.inf) if writers else math.inf
             t_out, steps, last_dt = C.c_double(), C.c_int64(), C.c_double()
@@ -715,4 +806,5 @@ def simulate_to_time(simulator: Simulator, endtime: float, *, match_endtime: boo
             simulator.t = float(np.float32(simulator.t) + np.float32(simulator.current_timestep))
         else:
             simulator.t += simulator.current_timestep
-        callback(simulator.t, simulator)
+        if callback is not None:
+            callback(simulator.t, simulator)

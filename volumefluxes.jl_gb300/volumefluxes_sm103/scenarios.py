@@ -59,9 +59,20 @@ class Scenario:
     bottom_source: bool = False
     friction_law: str = "bsa2012"   # friction_bsa2012 / friction_fcg2016 / friction_bh2021
     eq: dict = field(default_factory=dict)  # ShallowWaterEquations keywords (rho, g, depth_cutoff, ...)
+    bc: str = "wall"                # "wall" or "periodic"
+    reconstruction: str = "linear"  # "linear" or "none"
+    sources: list | None = None     # explicit source-term objects (overrides the flags above)
+    t0: float = 0.0
     meta: dict = field(default_factory=dict)
 
+    def grid(self) -> vf.CartesianGrid:
+        return vf.CartesianGrid(self.nx, self.ny, gc=2,
+                                boundary=vf.PeriodicBC() if self.bc == "periodic" else vf.WallBC(),
+                                extent=[list(self.extent[0]), list(self.extent[1])])
+
     def source_terms(self) -> list:
+        if self.sources is not None:
+            return list(self.sources)
         st = []
         if self.bottom_source:
             st.append(vf.SourceTermBottom())
@@ -73,8 +84,7 @@ class Scenario:
 
     def build(self, backend: vf.SM103Backend) -> vf.Simulator:
         """The scenario script, written against the reference's API."""
-        grid = vf.CartesianGrid(self.nx, self.ny, gc=2, boundary=vf.WallBC(), extent=[list(self.extent[0]),
-                                                                                        list(self.extent[1])])
+        grid = self.grid()
         bottom = vf.ConstantBottomTopography() if self.B is None else vf.BottomTopography2D(self.B, backend, grid)
         eq = vf.ShallowWaterEquations(bottom, **self.eq)
         friction = None
@@ -82,10 +92,10 @@ class Scenario:
             law = {"bsa2012": vf.friction_bsa2012, "fcg2016": vf.friction_fcg2016,
                    "bh2021": vf.friction_bh2021}[self.friction_law]
             friction = vf.ImplicitFriction(Cz=self.manning_n ** 2, friction_function=law)
-        system = vf.ConservedSystem(backend, vf.LinearReconstruction(self.theta), vf.CentralUpwind(eq), eq, grid,
-                                    self.source_terms(), friction)
+        rec = vf.NoReconstruction() if self.reconstruction == "none" else vf.LinearReconstruction(self.theta)
+        system = vf.ConservedSystem(backend, rec, vf.CentralUpwind(eq), eq, grid, self.source_terms(), friction)
         stepper = vf.RungeKutta2() if self.stepper == "rk2" else vf.ForwardEulerStepper()
-        sim = vf.Simulator(backend, system, stepper, grid, cfl=self.cfl)
+        sim = vf.Simulator(backend, system, stepper, grid, cfl=self.cfl, t0=self.t0)
         vf.set_current_state(sim, (self.w0, self.hu0, self.hv0))
         return sim
 
