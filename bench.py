@@ -60,6 +60,11 @@ def parse():
     ap.add_argument("--state-in", default=None, help="start from an interior state saved with --state-out")
     ap.add_argument("--cpu-budget", type=float, default=60.0,
                     help="seconds of oracle stepping the reference arm may spend (it runs min(K, budget) steps)")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--ensemble-members", type=int, default=256)
+    ap.add_argument("--ensemble-plain-budget", type=float, default=40.0,
+                    help="seconds the sequential plain baseline of the ensemble may spend (it runs a sample)")
+    ap.add_argument("--no-autotune", action="store_true", help="ensemble with the library's default granularity")
     return ap.parse_args()
 
 
@@ -318,6 +323,103 @@ def fp64_roofline(sc, ms_flux, ms_stage, clk_mhz, inst):
             "inst_source": "ncu DADD+DMUL+DFMA per cell, 3072^2 developed-flow capture"}
 
 
+def ensemble_workload(n):
+    return (f"batched ensemble: {n} flood scenarios, Float32, square side log-uniform in [64,1024] (Δ = 1 m), "
+            "8-32 seeded Gaussian hills (amplitude U[0.5,4] m, width U[50,400] m) + 1e-3 slope, uniform initial "
+            "depth U[0,2] m, rain U[0,5e-5] m/s, Manning n U[0.01,0.08] (bsa2012), wall BCs, RK2, CFL 0.25, "
+            "own CFL dt to an end time U[10,600] s each, depth_cutoff 8e-2 (examples/terrain.jl:92)")
+
+
+def measure_ensemble(args, local):
+    """The batched ensemble against the plain per-scenario drop-in on the same GPU.
+
+    Batch: every member from its initial state to its end time in one vf_batch
+    launch set, states resident on the device; latency of a member = time from
+    the launch until the host sees its done flag. Plain: simulate_to_time per
+    member, one after the other, on a sample of members (every m-th, time-boxed);
+    the sequential latencies for all members arriving at once are estimated from
+    the sample's mean time per member.
+    """
+    import volumefluxes_sm103 as vf
+    from volumefluxes_sm103 import ensemble as E
+    from volumefluxes_sm103 import scenarios as S
+    real = np.float32
+    specs = S.ensemble_specs(args.ensemble_members)
+    scen = [S.ensemble_member(s) for s in specs]
+    ends = [s.endtime for s in specs]
+    cells = np.array([sc.nx * sc.ny for sc in scen], dtype=np.float64)
+    be = vf.SM103Backend(real, device=local)
+    tuned, table = None, []
+    if not args.no_autotune:
+        probe = [sc.build(be) for sc in scen[::8]]
+        tuned, table = E.autotune(probe, steps=60)
+        for p in probe:
+            p.close()
+    sims = [sc.build(be) for sc in scen]
+    lib = sims[0]._lib
+    n0 = sum(s.launch_count() for s in sims)
+    done_at = [None] * len(sims)
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        run = E.BatchRun(sims, ends, options=tuned)
+        pending = set(range(len(sims)))
+        while pending:
+            for i in list(pending):
+                if run.is_done(i):
+                    done_at[i] = time.perf_counter() - t0
+                    pending.discard(i)
+            time.sleep(0.0005)
+        res = run.finish()
+        makespan = time.perf_counter() - t0
+    launches = sum(s.launch_count() for s in sims) - n0
+    steps = np.array([r.steps for r in res], dtype=np.float64)
+    status = [E.STATUS_NAMES[r.status] for r in res]
+    lat = np.array(done_at)
+    batch = {
+        "scenarios_per_s": len(sims) / makespan, "makespan_s": makespan,
+        "cell_updates_per_s": float((cells * steps).sum() / makespan),
+        "latency_s": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
+                      "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
+        "member_steps": {"min": int(steps.min()), "median": float(np.median(steps)), "max": int(steps.max()),
+                         "total": int(steps.sum())},
+        "status": {k: status.count(k) for k in sorted(set(status))},
+        "gpu_launches": launches, "clocks": clk.summary(),
+        "options": None if tuned is None else {k: v for k, v in tuned.__dict__.items() if v is not None},
+        "autotune_top": [[{k: v for k, v in c.__dict__.items() if v is not None}, r] for c, r in table[:4]],
+    }
+    # the plain drop-in, one member after the other, on a time-boxed sample
+    m = 8
+    sample, times, equal = [], [], 0
+    tb = time.perf_counter()
+    for i in range(0, len(scen), m):
+        if time.perf_counter() - tb > args.ensemble_plain_budget:
+            break
+        p = scen[i].build(be)
+        t1 = time.perf_counter()
+        vf.simulate_to_time(p, ends[i])
+        times.append(time.perf_counter() - t1)
+        sample.append(i)
+        equal += int(np.array_equal(vf.current_interior_state(p).h, vf.current_interior_state(sims[i]).h))
+        p.close()
+    for s in sims:
+        s.close()
+    mean_t = float(np.mean(times))
+    total_est = mean_t * len(scen)
+    plain = {
+        "scenarios_per_s": 1.0 / mean_t,
+        "cell_updates_per_s": float((cells[sample] * steps[sample]).sum() / np.sum(times)),
+        "makespan_s_est": total_est,
+        "latency_s_est": {"p50": 0.50 * total_est, "p95": 0.95 * total_est, "p99": 0.99 * total_est},
+        "sample": f"{len(sample)} of {len(scen)} members (every {m}th), simulate_to_time each, "
+                  f"{np.sum(times):.1f} s; all-at-once sequential latencies estimated from the mean per member",
+        "bitwise_equal_to_batch": f"{equal} of {len(sample)}",
+    }
+    return {"workload": ensemble_workload(len(scen)), "dtype": "f32", "members": len(scen), "batch": batch,
+            "plain_sequential": plain, "speedup_scenarios_per_s": batch["scenarios_per_s"] / plain["scenarios_per_s"],
+            "timing": "host wall clock from vf_batch_launch to each member's done flag (pinned mapped memory), "
+                      "states resident on the device"}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -363,6 +465,9 @@ def main():
         cpu = {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
                "sample": f"{steps} RK2 steps of the {sc.nx}x{sc.ny} Float64 workload from its initial state "
                          f"({el:.1f} s, OpenMP over rows)"}
+    ens = None
+    if rank == 0 and world == 1 and not args.no_ensemble:
+        ens = measure_ensemble(args, local)
     if rank != 0:
         return
     head = results[args.dtype]
@@ -377,6 +482,7 @@ def main():
         "compute_roofline": head.get("compute_roofline"),
         "cpu_baseline": cpu, "e2e": head["e2e"], "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
         "variants": {k: v for k, v in results.items() if k != args.dtype},
+        "ensemble": ens,
     }
     print(json.dumps(line), flush=True)
 

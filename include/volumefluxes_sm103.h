@@ -169,6 +169,66 @@ int vf_time_steps(vf_handle* h, int64_t n_steps, float* ms_out);
  * of the stage (RK2) or apply (forward Euler) passes. */
 int vf_time_kernels(vf_handle* h, int64_t n_steps, float* ms_flux, float* ms_stage);
 
+/* ---- Batched ensemble ------------------------------------------------------
+ * Advances many independent simulations, each a handle set up as above, each
+ * to its own end time with its own CFL dt: the loop of simulate_to_time
+ * (src/simulator.jl:179-212, with callback = nothing) run for every handle at
+ * once. The reference steps one Simulator at a time; these calls have no
+ * counterpart there and replace a host loop over simulate_to_time calls.
+ *
+ * One thread-block cluster per simulation runs its whole time loop on the
+ * device; launches are grouped by cluster size (one launch per group,
+ * concurrent streams), and the GPU's block scheduler starts a pending
+ * simulation whenever a cluster finishes. Per-handle results are bitwise
+ * those of vf_simulate on the same handle in Float64, and independent of
+ * which other simulations share the launch in both precisions. */
+#define VF_BATCH_OK 0          /* reached its end time */
+#define VF_BATCH_TIMEOUT 1     /* the launch's watchdog (time_limit_s) stopped it */
+#define VF_BATCH_STALLED 2     /* t + dt rounded to t: no progress possible */
+#define VF_BATCH_MAX_STEPS 3   /* stopped after max_steps steps */
+
+typedef struct vf_batch_options {
+  int32_t tiles_per_cta;   /* target 32x16 tiles per CTA when sizing a cluster; 0: default (16) */
+  int32_t max_cluster;     /* largest cluster (1..16); 0: default (16) */
+  double time_limit_s;     /* watchdog from the batch's start, in seconds; <= 0: default (600 s) */
+  int32_t seg_rows;        /* rows per strip segment of Float32 column-marching members
+                              (8..256); 0: 64, halved down to 8 until every warp has two */
+} vf_batch_options;
+
+typedef struct vf_batch vf_batch;
+
+/* Starts the batch and returns without waiting. The handles must have state
+ * (and bottom, tables, fields) uploaded, must be distinct, must live on one
+ * device, and must not be used by other calls until collected. t0[i] and
+ * endtime[i] are per handle; match_endtime and maximum_timestep (< 0: none)
+ * act as in vf_simulate; max_steps <= 0 means no limit. opt may be NULL. */
+int vf_batch_launch(vf_handle* const* hs, int32_t n, const double* t0, const double* endtime,
+                    int32_t match_endtime, double maximum_timestep, int64_t max_steps,
+                    const vf_batch_options* opt, vf_batch** out);
+/* Number of simulations of the batch that have finished (non-blocking). */
+int vf_batch_poll(vf_batch* b, int32_t* n_done);
+/* 1 if simulation i has finished, else 0 (non-blocking); negative on error. */
+int vf_batch_is_done(vf_batch* b, int32_t i);
+/* Hands a finished simulation back to its handle (its current state becomes
+ * the final state) and reports its final time, steps, last dt and
+ * VF_BATCH_* status (any pointer may be NULL). VF_ESTATE if not finished. */
+int vf_batch_collect(vf_batch* b, int32_t i, double* t_out, int64_t* steps_out, double* last_dt_out,
+                     int32_t* status_out);
+/* Blocks until every simulation of the batch has finished. */
+int vf_batch_wait(vf_batch* b);
+/* Waits, collects what is not collected yet, and frees the batch. */
+int vf_batch_free(vf_batch* b);
+/* launch + wait + collect every simulation + free. Outputs are arrays of n
+ * (any may be NULL). */
+int vf_batch_simulate(vf_handle* const* hs, int32_t n, const double* t0, const double* endtime,
+                      int32_t match_endtime, double maximum_timestep, int64_t max_steps,
+                      const vf_batch_options* opt, double* t_out, int64_t* steps_out, double* last_dt_out,
+                      int32_t* status_out);
+/* Cluster size the batch would give handle h under opt (NULL: defaults). */
+int vf_batch_cluster_size(vf_handle* h, const vf_batch_options* opt, int32_t* csize_out);
+/* Message for the last batch failure (b may be NULL for vf_batch_launch). */
+const char* vf_batch_last_error(vf_batch* b);
+
 /* Largest interior row count vf_water_volume_static accepts. */
 #define VF_STATIC_MAX_ROWS 16384
 

@@ -35,22 +35,23 @@ def test_library_exports_every_declared_symbol(lib):
     assert sorted(N.EXPORTED_SYMBOLS) == decl
 
 
-def test_config_struct_layout_matches_header(tmp_path):
+@pytest.mark.parametrize("ctype,cname", [(N.VfConfig, "vf_config"), (N.VfBatchOptions, "vf_batch_options")])
+def test_struct_layouts_match_header(tmp_path, ctype, cname):
     cc = shutil.which("gcc") or shutil.which("cc")
     if cc is None:
         pytest.skip("no C compiler")
-    fields = [f for f, _ in N.VfConfig._fields_]
+    fields = [f for f, _ in ctype._fields_]
     src = ["#include <stdio.h>", "#include <stddef.h>", '#include "volumefluxes_sm103.h"', "int main(void){",
-           'printf("%zu\\n", sizeof(vf_config));']
-    src += [f'printf("%zu\\n", offsetof(vf_config, {f}));' for f in fields]
+           f'printf("%zu\\n", sizeof({cname}));']
+    src += [f'printf("%zu\\n", offsetof({cname}, {f}));' for f in fields]
     src += ["return 0;}"]
     c = tmp_path / "layout.c"
     c.write_text("\n".join(src))
     exe = tmp_path / "layout"
     subprocess.run([cc, f"-I{ROOT / 'include'}", str(c), "-o", str(exe)], check=True)
     out = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
-    assert out[0] == ctypes.sizeof(N.VfConfig)
-    assert out[1:] == [getattr(N.VfConfig, f).offset for f in fields]
+    assert out[0] == ctypes.sizeof(ctype)
+    assert out[1:] == [getattr(ctype, f).offset for f in fields]
 
 
 def _cfg(**kw):
@@ -91,3 +92,16 @@ def test_null_handles_are_rejected(lib):
     assert lib.vf_step(None, 1.0, 0.0, None) == N.VF_EINVAL
     assert lib.vf_water_volume(None, None) == N.VF_EINVAL
     assert lib.vf_launch_count(None) == 0
+
+
+def test_batch_rejects_bad_arguments_without_touching_the_gpu(lib):
+    b = ctypes.c_void_p()
+    t = (ctypes.c_double * 1)(0.0)
+    assert lib.vf_batch_launch(None, 1, t, t, 1, -1.0, 0, None, ctypes.byref(b)) == N.VF_EINVAL
+    hs = (ctypes.c_void_p * 1)(None)
+    assert lib.vf_batch_launch(hs, 1, t, t, 1, -1.0, 0, None, ctypes.byref(b)) == N.VF_EINVAL
+    assert b"NULL handle" in lib.vf_batch_last_error(None)
+    assert lib.vf_batch_launch(hs, 0, t, t, 1, -1.0, 0, None, ctypes.byref(b)) == N.VF_EINVAL
+    assert not b.value
+    assert lib.vf_batch_poll(None, None) == N.VF_EINVAL
+    assert lib.vf_batch_free(None) == N.VF_OK

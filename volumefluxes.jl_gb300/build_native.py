@@ -1,12 +1,13 @@
 """Build libvfsm103.so, the sm_103a shallow-water step library, in-tree.
 
-Four translation units compile in parallel with nvcc and link into one shared
+Five translation units compile in parallel with nvcc and link into one shared
 library with the CUDA runtime linked statically:
 
   vf_f64.cu  Float64 kernels, -fmad=false (each operation rounds as in Julia)
   vf_f32.cu  Float32 kernels, contraction and fast division allowed
   vf_abi.cu  the extern "C" boundary of include/volumefluxes_sm103.h
   vf_noalloc.cu  the allocation-free water-volume entry point
+  vf_batch.cu  the batched-ensemble entry points
 
 Usage: python volumefluxes.jl_gb300/build_native.py [--force]
 """
@@ -33,6 +34,7 @@ UNITS = {
     "vf_f32.cu": ["-fmad=true", "-ftz=true", "-prec-sqrt=false"],
     "vf_abi.cu": [],
     "vf_noalloc.cu": [],
+    "vf_batch.cu": [],
 }
 
 

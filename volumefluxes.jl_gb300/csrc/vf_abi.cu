@@ -11,11 +11,11 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <new>
 #include <string>
 
-#include "../../include/volumefluxes_sm103.h"
-#include "vf_launch.cuh"
+#include "vf_handle.h"
 
 namespace {
 
@@ -27,36 +27,48 @@ long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
 
 namespace vf {
 void set_global_error(const char* msg) { g_create_error = msg; }
+
+cudaMemPool_t device_pool(int device) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  if (device < 0 || device >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!pools[device]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    unsigned long long keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[device] = pool;
+  }
+  return pools[device];
+}
 }  // namespace vf
 
-struct vf_handle {
-  vf_config cfg;
-  int device = 0;
-  size_t elem = 8;
-  cudaStream_t stream = nullptr;
-  int N1 = 0, N2 = 0;
-  long long P = 0, PS = 0, PB = 0;
-  void* U[2] = {nullptr, nullptr};
-  void* L = nullptr;
-  void* S = nullptr;
-  void* B = nullptr;
-  vf::StepRecord* rec = nullptr;
-  vf::StepRecord* rec_h = nullptr;
-  double* partial = nullptr;
-  double* vol_out = nullptr;
-  void* src_field[VF_MAX_SOURCES] = {};   // per-cell source arrays (state layout)
-  double* src_tab[VF_MAX_SOURCES] = {};   // breakpoints then rates/3600
-  int src_tab_n[VF_MAX_SOURCES] = {};
-  int vol_blocks = 0;
-  vf::StepArgs<double> ad;
-  vf::StepArgs<float> af;
-  bool have_state = false;
-  bool have_bottom = false;
-  std::string err;
-  long long launches = 0;
-};
-
 namespace {
+
+// Stream-ordered allocation from the library pool on the handle's stream.
+bool dalloc(vf_handle* h, void** p, size_t bytes) {
+  cudaMemPool_t pool = vf::device_pool(h->device);
+  if (!pool) return false;
+  if (cudaMallocFromPoolAsync(p, bytes, pool, h->stream) != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return false;
+  }
+  return true;
+}
+
+void dfree(vf_handle* h, void* p) {
+  if (p) cudaFreeAsync(p, h->stream);
+}
 
 int fail(vf_handle* h, int code, const std::string& msg) {
   if (h) h->err = msg;
@@ -288,25 +300,32 @@ int ensure_ready(vf_handle* h) {
 void destroy(vf_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
-  if (h->stream) cudaStreamSynchronize(h->stream);
-  cudaFree(h->U[0]);
-  cudaFree(h->U[1]);
-  cudaFree(h->L);
-  cudaFree(h->S);
-  cudaFree(h->B);
-  cudaFree(h->rec);
-  cudaFree(h->partial);
-  cudaFree(h->vol_out);
-  for (int i = 0; i < VF_MAX_SOURCES; ++i) {
-    cudaFree(h->src_field[i]);
-    cudaFree(h->src_tab[i]);
+  if (h->stream) {
+    cudaStreamSynchronize(h->stream);
+    dfree(h, h->U[0]);
+    dfree(h, h->U[1]);
+    dfree(h, h->L);
+    dfree(h, h->S);
+    dfree(h, h->B);
+    dfree(h, h->rec);
+    dfree(h, h->partial);
+    dfree(h, h->vol_out);
+    for (int i = 0; i < VF_MAX_SOURCES; ++i) {
+      dfree(h, h->src_field[i]);
+      dfree(h, h->src_tab[i]);
+    }
+    cudaStreamSynchronize(h->stream);
+    cudaStreamDestroy(h->stream);
   }
-  if (h->rec_h) cudaFreeHost(h->rec_h);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h->rec_h;
   delete h;
 }
 
 }  // namespace
+
+namespace vf {
+int handle_ready(vf_handle* h) { return ensure_ready(h); }
+}  // namespace vf
 
 extern "C" {
 
@@ -339,17 +358,17 @@ int vf_create(const vf_config* cfg, vf_handle** out) {
   }
   const size_t state_bytes = (size_t)(3 * h->PS) * h->elem;
   bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess;
-  ok = ok && cudaMalloc(&h->U[0], state_bytes) == cudaSuccess;
-  ok = ok && cudaMalloc(&h->U[1], state_bytes) == cudaSuccess;
-  ok = ok && cudaMalloc(&h->L, state_bytes) == cudaSuccess;
-  if (cfg->friction != VF_FRICTION_NONE) ok = ok && cudaMalloc(&h->S, (size_t)h->PS * h->elem) == cudaSuccess;
-  if (!cfg->bottom_is_constant)
-    ok = ok && cudaMalloc(&h->B, (size_t)(h->PB * (h->N2 + 1)) * h->elem) == cudaSuccess;
-  ok = ok && cudaMalloc(&h->rec, sizeof(vf::StepRecord)) == cudaSuccess;
-  ok = ok && cudaMallocHost(&h->rec_h, sizeof(vf::StepRecord)) == cudaSuccess;
+  ok = ok && dalloc(h, &h->U[0], state_bytes);
+  ok = ok && dalloc(h, &h->U[1], state_bytes);
+  ok = ok && dalloc(h, &h->L, state_bytes);
+  if (cfg->friction != VF_FRICTION_NONE) ok = ok && dalloc(h, &h->S, (size_t)h->PS * h->elem);
+  if (!cfg->bottom_is_constant) ok = ok && dalloc(h, &h->B, (size_t)(h->PB * (h->N2 + 1)) * h->elem);
+  ok = ok && dalloc(h, reinterpret_cast<void**>(&h->rec), sizeof(vf::StepRecord));
+  h->rec_h = new (std::nothrow) vf::StepRecord();
+  ok = ok && h->rec_h != nullptr;
   h->vol_blocks = 1024;
-  ok = ok && cudaMalloc(&h->partial, sizeof(double) * h->vol_blocks) == cudaSuccess;
-  ok = ok && cudaMalloc(&h->vol_out, sizeof(double)) == cudaSuccess;
+  ok = ok && dalloc(h, reinterpret_cast<void**>(&h->partial), sizeof(double) * h->vol_blocks);
+  ok = ok && dalloc(h, reinterpret_cast<void**>(&h->vol_out), sizeof(double));
   if (!ok) {
     cudaGetLastError();
     destroy(h);
@@ -425,11 +444,12 @@ int vf_set_source_table(vf_handle* h, int32_t index, const double* times, const 
     host[n + i] = rates[i] / 3600;  // compute_rain, src/sourceterms/source_term_rain.jl:53
   }
   if (h->src_tab[index] && h->src_tab_n[index] != n) {
-    cudaFree(h->src_tab[index]);
+    dfree(h, h->src_tab[index]);
     h->src_tab[index] = nullptr;
   }
   cudaError_t e = cudaSuccess;
-  if (!h->src_tab[index]) e = cudaMalloc(&h->src_tab[index], sizeof(double) * 2 * n);
+  if (!h->src_tab[index] && !dalloc(h, reinterpret_cast<void**>(&h->src_tab[index]), sizeof(double) * 2 * n))
+    e = cudaErrorMemoryAllocation;
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(h->src_tab[index], host, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -447,7 +467,7 @@ int vf_set_source_field(vf_handle* h, int32_t index, const void* field) {
     return fail(h, VF_EINVAL, "source index is not a HortonInfiltration or rain field");
   VF_CK(h, cudaSetDevice(h->device));
   if (!h->src_field[index]) {
-    VF_CK(h, cudaMalloc(&h->src_field[index], (size_t)h->PS * h->elem));
+    if (!dalloc(h, &h->src_field[index], (size_t)h->PS * h->elem)) return fail(h, VF_ENOMEM, "device allocation failed");
     VF_CK(h, cudaMemsetAsync(h->src_field[index], 0, (size_t)h->PS * h->elem, h->stream));
   }
   int rc = copy_planes(h, h->src_field[index], field, nullptr, 0, 0, h->N1, h->N2, 1, nullptr, nullptr);

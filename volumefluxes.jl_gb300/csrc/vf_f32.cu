@@ -17,5 +17,12 @@ cudaError_t launch_volume(const Geom<float>& g, const float* U, const float* B, 
                           double* out, cudaStream_t st) {
   return launch_volume_impl<float>(g, U, B, partial, nblocks, out, st);
 }
+cudaError_t launch_ensemble(const EnsItem<float>* items, const int* order, int n, int csize, int variant,
+                            unsigned long long time_limit_ns, cudaStream_t st) {
+  return launch_ensemble_impl<float>(items, order, n, csize, variant, time_limit_ns, st);
+}
+cudaError_t ensemble_max_clusters_f32(int csize, int variant, int* out) {
+  return ensemble_max_clusters_impl<float>(csize, variant, out);
+}
 cudaError_t configure_kernels_f32() { return configure_impl<float>(); }
 }  // namespace vf

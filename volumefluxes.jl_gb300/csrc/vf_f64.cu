@@ -18,5 +18,12 @@ cudaError_t launch_volume(const Geom<double>& g, const double* U, const double* 
                           double* out, cudaStream_t st) {
   return launch_volume_impl<double>(g, U, B, partial, nblocks, out, st);
 }
+cudaError_t launch_ensemble(const EnsItem<double>* items, const int* order, int n, int csize, int variant,
+                            unsigned long long time_limit_ns, cudaStream_t st) {
+  return launch_ensemble_impl<double>(items, order, n, csize, variant, time_limit_ns, st);
+}
+cudaError_t ensemble_max_clusters_f64(int csize, int variant, int* out) {
+  return ensemble_max_clusters_impl<double>(csize, variant, out);
+}
 cudaError_t configure_kernels_f64() { return configure_impl<double>(); }
 }  // namespace vf

@@ -77,6 +77,18 @@ __device__ __forceinline__ long long sidx(const Geom<T>& g, int x, int y) {
   return (long long)y * g.P + x + XOFF;
 }
 
+// Global load of step data. CG = true reads through L2 only (ld.global.cg): the
+// ensemble kernel reads fields that other CTAs of its cluster wrote earlier in
+// the same launch, which the read-only and L1 paths may not see.
+template <bool CG, typename T>
+__device__ __forceinline__ T gld(const T* ptr) {
+  if constexpr (CG) {
+    return __ldcg(ptr);
+  } else {
+    return *ptr;
+  }
+}
+
 // Bottom topography seen from a tile; (lx, ly) are tile-local cell coordinates,
 // corner (x0+lx, y0+ly) lives at sB[(ly+2)*BHX + lx+2]. Lookups follow
 // src/bottom_topography.jl:97-101.
@@ -127,19 +139,18 @@ __device__ __forceinline__ void no_reconstruction(const T c[3], T Bc, T L[3], T 
 template <typename T>
 __device__ __forceinline__ void stage1_point(const Phys<T>& p, T tdt, T u0, T u1, T u2, T l0, T l1, T l2, T S, T Bc,
                                              T& w, T& hu, T& hv);
-template <typename T>
-__device__ __forceinline__ void u1_global(const Geom<T>& g, const Phys<T>& p, T tdt, const T* __restrict__ U0,
-                                          const T* __restrict__ Lin, const T* __restrict__ Sin,
-                                          const T* __restrict__ B, int x, int y, T& w, T& hu, T& hv) {
+template <typename T, bool CG>
+__device__ __forceinline__ void u1_global(const Geom<T>& g, const Phys<T>& p, T tdt, const T* U0, const T* Lin,
+                                          const T* Sin, const T* __restrict__ B, int x, int y, T& w, T& hu, T& hv) {
   const long long o = sidx(g, x, y);
   T Bc = g.bconst;
   if (!g.bottom_const) {
     const long long b = (long long)y * g.PB + x + XOFF;
     Bc = (T)0.25 * (((B[b] + B[b + 1]) + B[b + g.PB]) + B[b + g.PB + 1]);
   }
-  const T S = p.friction ? Sin[o] : (T)0;
-  stage1_point<T>(p, tdt, U0[o], U0[g.PS + o], U0[2 * g.PS + o], Lin[o], Lin[g.PS + o], Lin[2 * g.PS + o], S, Bc, w,
-                  hu, hv);
+  const T S = p.friction ? gld<CG>(Sin + o) : (T)0;
+  stage1_point<T>(p, tdt, gld<CG>(U0 + o), gld<CG>(U0 + g.PS + o), gld<CG>(U0 + 2 * g.PS + o), gld<CG>(Lin + o),
+                  gld<CG>(Lin + g.PS + o), gld<CG>(Lin + 2 * g.PS + o), S, Bc, w, hu, hv);
 }
 
 // Time derivative of one stage on the tile held in sU (3 planes of HY x HX).
@@ -288,14 +299,13 @@ struct SmemFlux {
   T scal[8];
 };
 
-template <typename T>
-__global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_flux(Geom<T> g, Phys<T> p, const T* __restrict__ U, const T* __restrict__ B,
-                                             T* __restrict__ Lout, T* __restrict__ Sout, StepRecord* rec, int parity) {
-  if (!rec->active[parity]) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemFlux<T>& s = *reinterpret_cast<SmemFlux<T>*>(smem_raw);
+// Flux pass over one tile at (x0, y0) (block-collective): L(U0) and S(U0) to
+// global memory; mx, my accumulate this thread's share of the CFL maxima.
+// t is the step's start time (time-dependent sources).
+template <typename T, bool CG>
+__device__ __forceinline__ void flux_tile(const Geom<T>& g, const Phys<T>& p, const T* U, const T* __restrict__ B,
+                                          T* Lout, T* Sout, int x0, int y0, SmemFlux<T>& s, double t, T& mx, T& my) {
   const int tid = threadIdx.x;
-  const int x0 = g.gc + blockIdx.x * TX, y0 = g.gc + blockIdx.y * TY;
   const int nvx = min(TX, g.gc + g.nx - x0), nvy = min(TY, g.gc + g.ny - y0);
 
   for (int idx = tid; idx < HX * HY; idx += NT) {
@@ -304,15 +314,14 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_flux(Geom<T> g, Phys
     const bool ok = gx < g.N1 && gy < g.N2;
     const long long o = sidx(g, gx, gy);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) s.U[k * HX * HY + idx] = ok ? U[k * g.PS + o] : (T)0;
+    for (int k = 0; k < 3; ++k) s.U[k * HX * HY + idx] = ok ? gld<CG>(U + k * g.PS + o) : (T)0;
   }
   if (!g.bottom_const) load_corners(g, B, s.B, x0, y0);
-  if (p.any_dynamic && tid == 0) point_scalars<T>(p, rec->t[parity], s.scal);
+  if (p.any_dynamic && tid == 0) point_scalars<T>(p, t, s.scal);
   __syncthreads();
 
   BTile<T> bt{s.B, g.bottom_const, g.bconst};
   T acc[CPT][3];
-  T mx = (T)0, my = (T)0;
   tile_derivative<T, true>(p, s.U, bt, s.L, s.R, s.F, acc, mx, my, nvx, nvy);
 
 #pragma unroll
@@ -329,48 +338,100 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_flux(Geom<T> g, Phys
       Sout[o] = friction_factor<T>(p, s.U[ci], s.U[HX * HY + ci], s.U[2 * HX * HY + ci], bt.cell(lx, ly));
     }
   }
+}
 
-  // CFL maxima: warp shuffle, then one atomic per block and direction.
-  unsigned long long kx = speed_key<T>(mx), ky = speed_key<T>(my);
+// Block maximum of per-thread CFL speed keys (IEEE bit patterns of speeds
+// >= 0): warp shuffles, then one shared-memory pass; valid in thread 0.
+__device__ __forceinline__ void block_key_max(unsigned long long kx, unsigned long long ky,
+                                              unsigned long long (*red)[NT / 32], unsigned long long& kx_out,
+                                              unsigned long long& ky_out) {
+  const int tid = threadIdx.x;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     kx = max(kx, __shfl_xor_sync(0xffffffffu, kx, o));
     ky = max(ky, __shfl_xor_sync(0xffffffffu, ky, o));
   }
   if ((tid & 31) == 0) {
-    s.red[0][tid >> 5] = kx;
-    s.red[1][tid >> 5] = ky;
+    red[0][tid >> 5] = kx;
+    red[1][tid >> 5] = ky;
   }
   __syncthreads();
-  if (tid < 2) {
-    unsigned long long m = 0;
-    for (int w = 0; w < NT / 32; ++w) m = max(m, s.red[tid][w]);
-    atomicMax(&rec->speed_bits[parity][tid], m);
+  if (tid == 0) {
+    kx = 0;
+    ky = 0;
+    for (int w = 0; w < NT / 32; ++w) {
+      kx = max(kx, red[0][w]);
+      ky = max(ky, red[1][w]);
+    }
+    kx_out = kx;
+    ky_out = ky;
   }
 }
 
-// dt of stage 1, src/simulator.jl:147-150, and the time bookkeeping of
-// simulate_to_time (src/simulator.jl:199-205) for the step of this parity.
 template <typename T>
-__device__ __forceinline__ double step_dt(const Geom<T>& g, const StepRecord* rec, int parity) {
-  const double ax = speed_from_key<T>(rec->speed_bits[parity][0]);
-  const double ay = speed_from_key<T>(rec->speed_bits[parity][1]);
-  double max_dt;
-  if (rec->explicit_mode) {
-    max_dt = rec->explicit_max_dt;
-  } else {
-    max_dt = rec->match_endtime ? rec->endtime - rec->t[parity] : __longlong_as_double(0x7ff0000000000000ll);
-    if (rec->has_max_ts) max_dt = jmin<double>(max_dt, rec->max_ts);
+__device__ __forceinline__ void block_speed_keys(T mx, T my, unsigned long long (*red)[NT / 32],
+                                                 unsigned long long& kx_out, unsigned long long& ky_out) {
+  block_key_max(speed_key<T>(mx), speed_key<T>(my), red, kx_out, ky_out);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_flux(Geom<T> g, Phys<T> p, const T* __restrict__ U, const T* __restrict__ B,
+                                             T* __restrict__ Lout, T* __restrict__ Sout, StepRecord* rec, int parity) {
+  if (!rec->active[parity]) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SmemFlux<T>& s = *reinterpret_cast<SmemFlux<T>*>(smem_raw);
+  const int x0 = g.gc + blockIdx.x * TX, y0 = g.gc + blockIdx.y * TY;
+  const double t = p.any_dynamic ? rec->t[parity] : 0.0;
+  T mx = (T)0, my = (T)0;
+  flux_tile<T, false>(g, p, U, B, Lout, Sout, x0, y0, s, t, mx, my);
+
+  // CFL maxima: warp shuffle, then one atomic per block and direction.
+  unsigned long long kx = 0, ky = 0;
+  block_speed_keys<T>(mx, my, s.red, kx, ky);
+  if (threadIdx.x == 0) {
+    atomicMax(&rec->speed_bits[parity][0], kx);
+    atomicMax(&rec->speed_bits[parity][1], ky);
   }
+}
+
+// dt of stage 1 from the CFL maxima, src/simulator.jl:147-150.
+template <typename T>
+__device__ __forceinline__ double cfl_dt(const Geom<T>& g, double ax, double ay, double max_dt) {
   double dt = jmin<double>(g.cfl * jmin<double>(g.dx / ax, g.dy / ay), max_dt);
   if (sizeof(T) == 4) dt = (double)(float)dt;  // current_timestep is a MVector{1,Float32}
   return dt;
 }
 
+// The simulated time after a step (t += dt, src/simulator.jl:205, in the
+// backend's real type).
+template <typename T>
+__device__ __forceinline__ double next_time(double t, double dt) {
+  return sizeof(T) == 4 ? (double)((float)t + (float)dt) : t + dt;
+}
+
+// max_dt of simulate_to_time (src/simulator.jl:199-203).
+__device__ __forceinline__ double loop_max_dt(int match_endtime, double endtime, double t, int has_max_ts,
+                                              double max_ts) {
+  double max_dt = match_endtime ? endtime - t : __longlong_as_double(0x7ff0000000000000ll);
+  if (has_max_ts) max_dt = jmin<double>(max_dt, max_ts);
+  return max_dt;
+}
+
+// dt and time bookkeeping of the step of this parity.
+template <typename T>
+__device__ __forceinline__ double step_dt(const Geom<T>& g, const StepRecord* rec, int parity) {
+  const double ax = speed_from_key<T>(rec->speed_bits[parity][0]);
+  const double ay = speed_from_key<T>(rec->speed_bits[parity][1]);
+  const double max_dt = rec->explicit_mode
+                            ? rec->explicit_max_dt
+                            : loop_max_dt(rec->match_endtime, rec->endtime, rec->t[parity], rec->has_max_ts,
+                                          rec->max_ts);
+  return cfl_dt<T>(g, ax, ay, max_dt);
+}
+
 template <typename T>
 __device__ __forceinline__ void advance_record(StepRecord* rec, int parity, double dt) {
-  const double t = rec->t[parity];
-  double tn = sizeof(T) == 4 ? (double)((float)t + (float)dt) : t + dt;
+  const double tn = next_time<T>(rec->t[parity], dt);
   rec->last_dt = dt;
   rec->t[parity ^ 1] = tn;
   rec->n_done += 1;
@@ -461,26 +522,17 @@ struct SmemStage {
   T scal[8];
 };
 
-template <typename T>
-__global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_stage2(Geom<T> g, Phys<T> p, const T* __restrict__ U0, const T* __restrict__ B,
-                                               const T* __restrict__ Lin, const T* __restrict__ Sin, T* __restrict__ Uo,
-                                               StepRecord* rec, int parity) {
-  const bool root = blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0;
-  if (!rec->active[parity]) {
-    if (root) carry_record(rec, parity);
-    return;
-  }
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemStage<T>& s = *reinterpret_cast<SmemStage<T>*>(smem_raw);
+// RK2 stage pass over one tile at (x0, y0) (block-collective): U2 with its
+// ghosts into Uo. dt is the step's dt, t its start time.
+template <typename T, bool CG>
+__device__ __forceinline__ void stage2_tile(const Geom<T>& g, const Phys<T>& p, const T* U0, const T* __restrict__ B,
+                                            const T* Lin, const T* Sin, T* Uo, int x0, int y0, SmemStage<T>& s,
+                                            double dt, double t) {
   const int tid = threadIdx.x;
-  const int x0 = g.gc + blockIdx.x * TX, y0 = g.gc + blockIdx.y * TY;
   const int nvx = min(TX, g.gc + g.nx - x0), nvy = min(TY, g.gc + g.ny - y0);
-
-  if (tid == 0) s.dt = step_dt<T>(g, rec, parity);
-  if (p.any_dynamic && tid == 1) point_scalars<T>(p, rec->t[parity], s.scal);
+  if (p.any_dynamic && tid == 1) point_scalars<T>(p, t, s.scal);
   if (!g.bottom_const) load_corners(g, B, s.B, x0, y0);
   __syncthreads();
-  const double dt = s.dt;
   const T tdt = (T)dt;
   BTile<T> bt{s.B, g.bottom_const, g.bconst};
 
@@ -495,9 +547,10 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_stage2(Geom<T> g, Ph
     T w = (T)0, hu = (T)0, hv = (T)0;
     if (xin && yin) {
       const long long o = sidx(g, gx, gy);
-      const T a0 = U0[o], a1 = U0[g.PS + o], a2 = U0[2 * g.PS + o];
-      const T S = p.friction ? Sin[o] : (T)0;
-      stage1_point<T>(p, tdt, a0, a1, a2, Lin[o], Lin[g.PS + o], Lin[2 * g.PS + o], S, bt.cell(lx, ly), w, hu, hv);
+      const T a0 = gld<CG>(U0 + o), a1 = gld<CG>(U0 + g.PS + o), a2 = gld<CG>(U0 + 2 * g.PS + o);
+      const T S = p.friction ? gld<CG>(Sin + o) : (T)0;
+      stage1_point<T>(p, tdt, a0, a1, a2, gld<CG>(Lin + o), gld<CG>(Lin + g.PS + o), gld<CG>(Lin + 2 * g.PS + o), S,
+                      bt.cell(lx, ly), w, hu, hv);
       if (lx >= 0 && lx < TX && ly >= 0 && ly < TY) {
         const int t = ly * TX + lx;
         s.U0[t] = a0;
@@ -505,10 +558,10 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_stage2(Geom<T> g, Ph
         s.U0[2 * TX * TY + t] = a2;
       }
     } else if (yin && gx < g.N1) {
-      u1_global<T>(g, p, tdt, U0, Lin, Sin, B, bc_source(gx, g.gc, g.nx, g.bc), gy, w, hu, hv);
+      u1_global<T, CG>(g, p, tdt, U0, Lin, Sin, B, bc_source(gx, g.gc, g.nx, g.bc), gy, w, hu, hv);
       if (g.bc != 2) hu = -hu;
     } else if (xin && gy < g.N2) {
-      u1_global<T>(g, p, tdt, U0, Lin, Sin, B, gx, bc_source(gy, g.gc, g.ny, g.bc), w, hu, hv);
+      u1_global<T, CG>(g, p, tdt, U0, Lin, Sin, B, gx, bc_source(gy, g.gc, g.ny, g.bc), w, hu, hv);
       if (g.bc != 2) hv = -hv;
     }
     s.U1[idx] = w;
@@ -541,11 +594,53 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_stage2(Geom<T> g, Ph
     dry_clamp<T>(p, w, hu, hv, Bc);
     store_with_ghosts<T>(g, Uo, x0 + lx, y0 + ly, w, hu, hv);
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_stage2(Geom<T> g, Phys<T> p, const T* __restrict__ U0, const T* __restrict__ B,
+                                               const T* __restrict__ Lin, const T* __restrict__ Sin, T* __restrict__ Uo,
+                                               StepRecord* rec, int parity) {
+  const bool root = blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0;
+  if (!rec->active[parity]) {
+    if (root) carry_record(rec, parity);
+    return;
+  }
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SmemStage<T>& s = *reinterpret_cast<SmemStage<T>*>(smem_raw);
+  const int x0 = g.gc + blockIdx.x * TX, y0 = g.gc + blockIdx.y * TY;
+  if (threadIdx.x == 0) s.dt = step_dt<T>(g, rec, parity);
+  __syncthreads();
+  const double dt = s.dt;
+  stage2_tile<T, false>(g, p, U0, B, Lin, Sin, Uo, x0, y0, s, dt, rec->t[parity]);
   if (root) advance_record<T>(rec, parity, dt);
 }
 
 // ---------------------------------------------------------------------------
 // Forward-Euler apply pass: U1 = clamp((U0 + dt*L) ./ (1 .- dt*[0,S,S])).
+// Forward-Euler apply over one tile at (x0, y0): the pointwise stage-1 update.
+template <typename T, bool CG>
+__device__ __forceinline__ void apply_fe_tile(const Geom<T>& g, const Phys<T>& p, const T* U0,
+                                              const T* __restrict__ B, const T* Lin, const T* Sin, T* Uo, int x0,
+                                              int y0, double dt) {
+  const T tdt = (T)dt;
+  const int lx = threadIdx.x % TX, ly0 = threadIdx.x / TX;
+  for (int ly = ly0; ly < TY; ly += NT / TX) {
+    const int gx = x0 + lx, gy = y0 + ly;
+    if (gx >= g.gc + g.nx || gy >= g.gc + g.ny) continue;
+    const long long o = sidx(g, gx, gy);
+    T Bc = g.bconst;
+    if (!g.bottom_const) {
+      const long long b = (long long)gy * g.PB + gx + XOFF;
+      Bc = (T)0.25 * (((B[b] + B[b + 1]) + B[b + g.PB]) + B[b + g.PB + 1]);
+    }
+    const T S = p.friction ? gld<CG>(Sin + o) : (T)0;
+    T w, hu, hv;
+    stage1_point<T>(p, tdt, gld<CG>(U0 + o), gld<CG>(U0 + g.PS + o), gld<CG>(U0 + 2 * g.PS + o), gld<CG>(Lin + o),
+                    gld<CG>(Lin + g.PS + o), gld<CG>(Lin + 2 * g.PS + o), S, Bc, w, hu, hv);
+    store_with_ghosts<T>(g, Uo, gx, gy, w, hu, hv);
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NT) k_apply_fe(Geom<T> g, Phys<T> p, const T* __restrict__ U0,
                                                  const T* __restrict__ B, const T* __restrict__ Lin,
@@ -560,23 +655,7 @@ __global__ void __launch_bounds__(NT) k_apply_fe(Geom<T> g, Phys<T> p, const T* 
   if (threadIdx.x == 0) sdt = step_dt<T>(g, rec, parity);
   __syncthreads();
   const double dt = sdt;
-  const T tdt = (T)dt;
-  const int lx = threadIdx.x % TX, ly0 = threadIdx.x / TX;
-  for (int ly = ly0; ly < TY; ly += NT / TX) {
-    const int gx = g.gc + blockIdx.x * TX + lx, gy = g.gc + blockIdx.y * TY + ly;
-    if (gx >= g.gc + g.nx || gy >= g.gc + g.ny) continue;
-    const long long o = sidx(g, gx, gy);
-    T Bc = g.bconst;
-    if (!g.bottom_const) {
-      const long long b = (long long)gy * g.PB + gx + XOFF;
-      Bc = (T)0.25 * (((B[b] + B[b + 1]) + B[b + g.PB]) + B[b + g.PB + 1]);
-    }
-    const T S = p.friction ? Sin[o] : (T)0;
-    T w, hu, hv;
-    stage1_point<T>(p, tdt, U0[o], U0[g.PS + o], U0[2 * g.PS + o], Lin[o], Lin[g.PS + o], Lin[2 * g.PS + o], S, Bc, w,
-                    hu, hv);
-    store_with_ghosts<T>(g, Uo, gx, gy, w, hu, hv);
-  }
+  apply_fe_tile<T, false>(g, p, U0, B, Lin, Sin, Uo, g.gc + blockIdx.x * TX, g.gc + blockIdx.y * TY, dt);
   if (root) advance_record<T>(rec, parity, dt);
 }
 

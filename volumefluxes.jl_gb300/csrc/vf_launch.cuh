@@ -2,6 +2,7 @@
 // type. The Float64 set lives in vf_f64.cu (built with -fmad=false so every
 // expression rounds as in Julia), the Float32 set in vf_f32.cu.
 #pragma once
+#include "vf_ensemble.cuh"
 #include "vf_march.cuh"
 
 namespace vf {
@@ -34,6 +35,15 @@ cudaError_t launch_volume(const Geom<double>& g, const double* U, const double* 
                           double* out_dev, cudaStream_t st);
 cudaError_t launch_volume(const Geom<float>& g, const float* U, const float* B, double* partial, int nblocks,
                           double* out_dev, cudaStream_t st);
+// Ensemble launch: n scenarios (items[order[i]]), one cluster of csize CTAs
+// each; variant 0 column marching (Float32 only), 1 tiles.
+cudaError_t launch_ensemble(const EnsItem<double>* items, const int* order, int n, int csize, int variant,
+                            unsigned long long time_limit_ns, cudaStream_t st);
+cudaError_t launch_ensemble(const EnsItem<float>* items, const int* order, int n, int csize, int variant,
+                            unsigned long long time_limit_ns, cudaStream_t st);
+// Clusters of csize CTAs that fit on the device at once (0: csize not launchable).
+cudaError_t ensemble_max_clusters_f64(int csize, int variant, int* out);
+cudaError_t ensemble_max_clusters_f32(int csize, int variant, int* out);
 // Opt the big-shared-memory kernels in on the current device (idempotent).
 cudaError_t configure_kernels_f64();
 cudaError_t configure_kernels_f32();

@@ -39,19 +39,24 @@ struct StripGeom {
   bool ld_col;         // column inside the stored array
 };
 
+// Strip `strip`, row segment `seg` (of seg_rows rows) for the calling warp.
 template <typename T>
-__device__ __forceinline__ bool strip_setup(const Geom<T>& g, int seg_rows, StripGeom& s) {
+__device__ __forceinline__ bool strip_setup_at(const Geom<T>& g, int seg_rows, int strip, int seg, StripGeom& s) {
   s.lane = threadIdx.x & (MW - 1);
-  const int strip = blockIdx.x * MWPB + (threadIdx.x >> 5);
   const int nstrips = (g.nx + MOUT - 1) / MOUT;
   if (strip >= nstrips) return false;
   s.xs = g.gc + strip * MOUT;
   s.x = s.xs - 2 + s.lane;
-  s.ys = g.gc + blockIdx.y * seg_rows;
+  s.ys = g.gc + seg * seg_rows;
   s.ye = min(s.ys + seg_rows, g.gc + g.ny);
   s.out_col = s.lane >= 2 && s.lane < 2 + MOUT && s.x < g.gc + g.nx;
   s.ld_col = s.x < g.N1;
   return true;
+}
+
+template <typename T>
+__device__ __forceinline__ bool strip_setup(const Geom<T>& g, int seg_rows, StripGeom& s) {
+  return strip_setup_at(g, seg_rows, (int)(blockIdx.x * MWPB + (threadIdx.x >> 5)), (int)blockIdx.y, s);
 }
 
 // Bottom corners (x, r) and (x+1, r) of one corner row.
@@ -97,14 +102,14 @@ struct Cell3 {
   T w, hu, hv;
 };
 
-template <typename T>
-__device__ __forceinline__ Cell3<T> load_cell(const Geom<T>& g, const T* __restrict__ U, int x, int r, bool ok) {
+template <typename T, bool CG>
+__device__ __forceinline__ Cell3<T> load_cell(const Geom<T>& g, const T* U, int x, int r, bool ok) {
   Cell3<T> c{(T)0, (T)0, (T)0};
   if (ok && r < g.N2) {
     const long long o = sidx(g, x, r);
-    c.w = U[o];
-    c.hu = U[g.PS + o];
-    c.hv = U[2 * g.PS + o];
+    c.w = gld<CG>(U + o);
+    c.hu = gld<CG>(U + g.PS + o);
+    c.hv = gld<CG>(U + 2 * g.PS + o);
   }
   return c;
 }
@@ -188,98 +193,103 @@ __device__ __forceinline__ void block_speed_commit(StepRecord* rec, int parity, 
 }
 
 // ---------------------------------------------------------------------------
+// Flux pass of one strip segment (warp-collective): L(U0), S(U0); mx, my
+// collect the warp's CFL maxima as bit-pattern keys.
+template <typename T, bool CG>
+__device__ __forceinline__ void flux_march_unit(const Geom<T>& g, const Phys<T>& p, const T* U,
+                                                const T* __restrict__ B, T* Lout, T* Sout, const StripGeom& s,
+                                                unsigned long long& mx, unsigned long long& my) {
+  const int x = s.x;
+  // prologue: rows ys-2..ys+1, corner rows ys-1..ys+2
+  const Cell3<T> um2 = load_cell<T, CG>(g, U, x, s.ys - 2, s.ld_col);
+  const Cell3<T> um1 = load_cell<T, CG>(g, U, x, s.ys - 1, s.ld_col);
+  Cell3<T> uc = load_cell<T, CG>(g, U, x, s.ys, s.ld_col);
+  Cell3<T> un = load_cell<T, CG>(g, U, x, s.ys + 1, s.ld_col);
+  const CornerRow<T> cm1 = load_corner_row(g, B, x, s.ys - 1);
+  CornerRow<T> c0 = load_corner_row(g, B, x, s.ys);
+  CornerRow<T> c1 = load_corner_row(g, B, x, s.ys + 1);
+  YCarry<T> y;
+  {
+    Cell3<T> Lm, Rm, L0, R0;
+    const T blm = b_yface(g, cm1), b0 = b_yface(g, c0), b1 = b_yface(g, c1);
+    recon<T>(p, um2, um1, uc, blm, b0, Lm, Rm);  // row ys-1
+    recon<T>(p, um1, uc, un, b0, b1, L0, R0);    // row ys
+    T sp = (T)0;
+    y.Gm = face<T, 1, true>(p, Rm, L0, sp);
+    if (s.out_col) my = max(my, speed_key<T>(sp));
+    y.R = R0;
+    y.Lh = L0.w;
+    y.Bl = b0;
+    y.Br = b1;
+  }
+  for (int j = s.ys; j < s.ye; ++j) {
+    const Cell3<T> u2 = load_cell<T, CG>(g, U, x, j + 2, s.ld_col);
+    const CornerRow<T> c2 = load_corner_row(g, B, x, j + 2);
+    T sx = (T)0;
+    Cell3<T> acc = x_derivative<T, true>(g, p, uc, c0, c1, sx);
+    if (s.lane >= 2 && s.lane <= 2 + MOUT && s.x <= g.gc + g.nx) mx = max(mx, speed_key<T>(sx));
+    // y: reconstruct row j+1, flux through face j+1/2
+    Cell3<T> Ln, Rn;
+    const T b2 = b_yface(g, c2);
+    recon<T>(p, uc, un, u2, y.Br, b2, Ln, Rn);
+    T sp = (T)0;
+    const Cell3<T> Gp = face<T, 1, true>(p, y.R, Ln, sp);
+    if (s.out_col) my = max(my, speed_key<T>(sp));
+    acc.w = acc.w - p.inv_dy * (Gp.w - y.Gm.w);
+    acc.hu = acc.hu - p.inv_dy * (Gp.hu - y.Gm.hu);
+    acc.hv = acc.hv - p.inv_dy * (Gp.hv - y.Gm.hv);
+    for (int b = 0; b < p.n_bottom; ++b)
+      acc.hv = acc.hv + p.neg_g * slope_over<T>(y.Br - y.Bl, p.dy, p.inv_dy, p.dy_pow2) * ((y.R.w + y.Lh) * (T)0.5);
+    acc.w = add_point_sources<T>(p, acc.w);
+    if (s.out_col) {
+      const long long o = sidx(g, x, j);
+      Lout[o] = acc.w;
+      Lout[g.PS + o] = acc.hu;
+      Lout[2 * g.PS + o] = acc.hv;
+      if (p.friction) {
+        T S = (T)0;
+        if (friction_active<T>(uc.hu, uc.hv)) S = friction_factor<T>(p, uc.w, uc.hu, uc.hv, b_cell(g, c0, c1));
+        Sout[o] = S;
+      }
+    }
+    // shift the window
+    uc = un;
+    un = u2;
+    c0 = c1;
+    c1 = c2;
+    y.R = Rn;
+    y.Lh = Ln.w;
+    y.Bl = y.Br;
+    y.Br = b2;
+    y.Gm = Gp;
+  }
+}
+
 template <typename T, int SEG>
 __global__ void __launch_bounds__(MW * MWPB) k_flux_march(Geom<T> g, Phys<T> p, const T* __restrict__ U,
                                                           const T* __restrict__ B, T* __restrict__ Lout,
                                                           T* __restrict__ Sout, StepRecord* rec, int parity) {
   if (!rec->active[parity]) return;
   StripGeom s;
-  const bool active = strip_setup(g, SEG, s);
   unsigned long long mx = 0ull, my = 0ull;  // CFL maxima as bit patterns (speeds are >= 0)
-  if (active) {
-    const int x = s.x;
-    // prologue: rows ys-2..ys+1, corner rows ys-1..ys+2
-    const Cell3<T> um2 = load_cell(g, U, x, s.ys - 2, s.ld_col);
-    const Cell3<T> um1 = load_cell(g, U, x, s.ys - 1, s.ld_col);
-    Cell3<T> uc = load_cell(g, U, x, s.ys, s.ld_col);
-    Cell3<T> un = load_cell(g, U, x, s.ys + 1, s.ld_col);
-    const CornerRow<T> cm1 = load_corner_row(g, B, x, s.ys - 1);
-    CornerRow<T> c0 = load_corner_row(g, B, x, s.ys);
-    CornerRow<T> c1 = load_corner_row(g, B, x, s.ys + 1);
-    YCarry<T> y;
-    {
-      Cell3<T> Lm, Rm, L0, R0;
-      const T blm = b_yface(g, cm1), b0 = b_yface(g, c0), b1 = b_yface(g, c1);
-      recon<T>(p, um2, um1, uc, blm, b0, Lm, Rm);  // row ys-1
-      recon<T>(p, um1, uc, un, b0, b1, L0, R0);    // row ys
-      T sp = (T)0;
-      y.Gm = face<T, 1, true>(p, Rm, L0, sp);
-      if (s.out_col) my = max(my, speed_key<T>(sp));
-      y.R = R0;
-      y.Lh = L0.w;
-      y.Bl = b0;
-      y.Br = b1;
-    }
-    for (int j = s.ys; j < s.ye; ++j) {
-      const Cell3<T> u2 = load_cell(g, U, x, j + 2, s.ld_col);
-      const CornerRow<T> c2 = load_corner_row(g, B, x, j + 2);
-      T sx = (T)0;
-      Cell3<T> acc = x_derivative<T, true>(g, p, uc, c0, c1, sx);
-      if (s.lane >= 2 && s.lane <= 2 + MOUT && s.x <= g.gc + g.nx) mx = max(mx, speed_key<T>(sx));
-      // y: reconstruct row j+1, flux through face j+1/2
-      Cell3<T> Ln, Rn;
-      const T b2 = b_yface(g, c2);
-      recon<T>(p, uc, un, u2, y.Br, b2, Ln, Rn);
-      T sp = (T)0;
-      const Cell3<T> Gp = face<T, 1, true>(p, y.R, Ln, sp);
-      if (s.out_col) my = max(my, speed_key<T>(sp));
-      acc.w = acc.w - p.inv_dy * (Gp.w - y.Gm.w);
-      acc.hu = acc.hu - p.inv_dy * (Gp.hu - y.Gm.hu);
-      acc.hv = acc.hv - p.inv_dy * (Gp.hv - y.Gm.hv);
-      for (int b = 0; b < p.n_bottom; ++b)
-        acc.hv = acc.hv + p.neg_g * slope_over<T>(y.Br - y.Bl, p.dy, p.inv_dy, p.dy_pow2) * ((y.R.w + y.Lh) * (T)0.5);
-      acc.w = add_point_sources<T>(p, acc.w);
-      if (s.out_col) {
-        const long long o = sidx(g, x, j);
-        Lout[o] = acc.w;
-        Lout[g.PS + o] = acc.hu;
-        Lout[2 * g.PS + o] = acc.hv;
-        if (p.friction) {
-          T S = (T)0;
-          if (friction_active<T>(uc.hu, uc.hv)) S = friction_factor<T>(p, uc.w, uc.hu, uc.hv, b_cell(g, c0, c1));
-          Sout[o] = S;
-        }
-      }
-      // shift the window
-      uc = un;
-      un = u2;
-      c0 = c1;
-      c1 = c2;
-      y.R = Rn;
-      y.Lh = Ln.w;
-      y.Bl = y.Br;
-      y.Br = b2;
-      y.Gm = Gp;
-    }
-  }
+  if (strip_setup(g, SEG, s)) flux_march_unit<T, false>(g, p, U, B, Lout, Sout, s, mx, my);
   block_speed_commit(rec, parity, mx, my);
 }
 
 // U1 of one loaded row for this lane (stage-1 update + dry clamp), before ghost mirroring.
-template <typename T>
-__device__ __forceinline__ Cell3<T> stage1_row(const Geom<T>& g, const Phys<T>& p, T tdt, const T* __restrict__ U0,
-                                               const T* __restrict__ Lin, const T* __restrict__ Sin, int x, int r,
-                                               bool xin, const CornerRow<T>& clo, const CornerRow<T>& chi,
-                                               Cell3<T>& u0out) {
+template <typename T, bool CG>
+__device__ __forceinline__ Cell3<T> stage1_row(const Geom<T>& g, const Phys<T>& p, T tdt, const T* U0, const T* Lin,
+                                               const T* Sin, int x, int r, bool xin, const CornerRow<T>& clo,
+                                               const CornerRow<T>& chi, Cell3<T>& u0out) {
   Cell3<T> u1{(T)0, (T)0, (T)0};
   u0out = Cell3<T>{(T)0, (T)0, (T)0};
   const bool yin = r >= g.gc && r < g.gc + g.ny;
   if (xin && yin) {
     const long long o = sidx(g, x, r);
-    u0out = Cell3<T>{U0[o], U0[g.PS + o], U0[2 * g.PS + o]};
-    const T S = p.friction ? Sin[o] : (T)0;
-    stage1_point<T>(p, tdt, u0out.w, u0out.hu, u0out.hv, Lin[o], Lin[g.PS + o], Lin[2 * g.PS + o], S,
-                    b_cell(g, clo, chi), u1.w, u1.hu, u1.hv);
+    u0out = Cell3<T>{gld<CG>(U0 + o), gld<CG>(U0 + g.PS + o), gld<CG>(U0 + 2 * g.PS + o)};
+    const T S = p.friction ? gld<CG>(Sin + o) : (T)0;
+    stage1_point<T>(p, tdt, u0out.w, u0out.hu, u0out.hv, gld<CG>(Lin + o), gld<CG>(Lin + g.PS + o),
+                    gld<CG>(Lin + 2 * g.PS + o), S, b_cell(g, clo, chi), u1.w, u1.hu, u1.hv);
   }
   return u1;
 }
@@ -309,6 +319,105 @@ __device__ __forceinline__ Cell3<T> mirror_row(const Cell3<T>& src) {  // src/bc
   return Cell3<T>{src.w, src.hu, -src.hv};
 }
 
+// RK2 stage pass of one strip segment (warp-collective): U2 with its ghosts into Uo.
+template <typename T, bool CG>
+__device__ __forceinline__ void stage_march_unit(const Geom<T>& g, const Phys<T>& p, const T* U0,
+                                                 const T* __restrict__ B, const T* Lin, const T* Sin, T* Uo,
+                                                 const StripGeom& s, T tdt) {
+  const int x = s.x;
+  const bool xin = x >= g.gc && x < g.gc + g.nx;
+  const int top = g.gc + g.ny;  // first top ghost row
+  // prologue: corner rows ys-2..ys+2, U1 rows ys-2..ys+1
+  const CornerRow<T> cm2 = load_corner_row(g, B, x, s.ys - 2);
+  const CornerRow<T> cm1 = load_corner_row(g, B, x, s.ys - 1);
+  CornerRow<T> c0 = load_corner_row(g, B, x, s.ys);
+  CornerRow<T> c1 = load_corner_row(g, B, x, s.ys + 1);
+  CornerRow<T> c2 = load_corner_row(g, B, x, s.ys + 2);
+  Cell3<T> u0c{(T)0, (T)0, (T)0}, u0n{(T)0, (T)0, (T)0}, dummy;
+  Cell3<T> uc = mirror_columns(g, s, stage1_row<T, CG>(g, p, tdt, U0, Lin, Sin, x, s.ys, xin, c0, c1, u0c), true);
+  Cell3<T> un;
+  if (s.ys + 1 >= top) {
+    un = mirror_row(uc);  // top ghost above a one-row segment
+  } else {
+    un = mirror_columns(g, s, stage1_row<T, CG>(g, p, tdt, U0, Lin, Sin, x, s.ys + 1, xin, c1, c2, u0n), true);
+  }
+  Cell3<T> um1, um2;
+  if (s.ys == g.gc) {  // bottom ghosts mirror rows gc, gc+1
+    um1 = mirror_row(uc);
+    um2 = mirror_row(un);
+  } else {
+    um1 = mirror_columns(g, s, stage1_row<T, CG>(g, p, tdt, U0, Lin, Sin, x, s.ys - 1, xin, cm1, c0, dummy), true);
+    um2 = mirror_columns(g, s, stage1_row<T, CG>(g, p, tdt, U0, Lin, Sin, x, s.ys - 2, xin, cm2, cm1, dummy), true);
+  }
+  // Ghost row top+1 mirrors row top-2, which leaves the window before it is needed.
+  Cell3<T> stash{(T)0, (T)0, (T)0};
+  if (s.ys + 1 == top) stash = mirror_row(um1);
+  YCarry<T> y;
+  {
+    Cell3<T> Lm, Rm, L0, R0;
+    const T blm = b_yface(g, cm1), b0 = b_yface(g, c0), b1 = b_yface(g, c1);
+    recon<T>(p, um2, um1, uc, blm, b0, Lm, Rm);
+    recon<T>(p, um1, uc, un, b0, b1, L0, R0);
+    T sp;
+    y.Gm = face<T, 1, false>(p, Rm, L0, sp);
+    y.R = R0;
+    y.Lh = L0.w;
+    y.Bl = b0;
+    y.Br = b1;
+  }
+  for (int j = s.ys; j < s.ye; ++j) {
+    // U1 of row j+2 (needs corner rows j+2, j+3)
+    const CornerRow<T> c3 = load_corner_row(g, B, x, j + 3);
+    Cell3<T> u2, u0x{(T)0, (T)0, (T)0};
+    if (j + 2 == top) {
+      u2 = mirror_row(un);     // row top mirrors top-1
+      stash = mirror_row(uc);  // row top+1 mirrors top-2
+    } else if (j + 2 == top + 1) {
+      u2 = stash;
+    } else {
+      u2 = mirror_columns(g, s, stage1_row<T, CG>(g, p, tdt, U0, Lin, Sin, x, j + 2, xin, c2, c3, u0x), j + 2 < top);
+    }
+    T sx;
+    Cell3<T> acc = x_derivative<T, false>(g, p, uc, c0, c1, sx);
+    Cell3<T> Ln, Rn;
+    const T b2 = b_yface(g, c2);
+    recon<T>(p, uc, un, u2, y.Br, b2, Ln, Rn);
+    T sp;
+    const Cell3<T> Gp = face<T, 1, false>(p, y.R, Ln, sp);
+    acc.w = acc.w - p.inv_dy * (Gp.w - y.Gm.w);
+    acc.hu = acc.hu - p.inv_dy * (Gp.hu - y.Gm.hu);
+    acc.hv = acc.hv - p.inv_dy * (Gp.hv - y.Gm.hv);
+    for (int b = 0; b < p.n_bottom; ++b)
+      acc.hv = acc.hv + p.neg_g * slope_over<T>(y.Br - y.Bl, p.dy, p.inv_dy, p.dy_pow2) * ((y.R.w + y.Lh) * (T)0.5);
+    acc.w = add_point_sources<T>(p, acc.w);
+    if (s.out_col) {
+      T w = uc.w + tdt * acc.w;
+      T hu = uc.hu + tdt * acc.hu;
+      T hv = uc.hv + tdt * acc.hv;
+      w = (T)0.5 * (u0c.w + w);
+      hu = (T)0.5 * (u0c.hu + hu);
+      hv = (T)0.5 * (u0c.hv + hv);
+      const T Bc = b_cell(g, c0, c1);
+      if (p.friction && friction_active<T>(uc.hu, uc.hv))
+        apply_friction<T>(tdt, friction_factor<T>(p, uc.w, uc.hu, uc.hv, Bc), hu, hv);
+      dry_clamp<T>(p, w, hu, hv, Bc);
+      store_with_ghosts<T>(g, Uo, x, j, w, hu, hv);
+    }
+    uc = un;
+    un = u2;
+    u0c = u0n;
+    u0n = u0x;
+    c0 = c1;
+    c1 = c2;
+    c2 = c3;
+    y.R = Rn;
+    y.Lh = Ln.w;
+    y.Bl = y.Br;
+    y.Br = b2;
+    y.Gm = Gp;
+  }
+}
+
 template <typename T, int SEG>
 __global__ void __launch_bounds__(MW * MWPB) k_stage_march(Geom<T> g, Phys<T> p, const T* __restrict__ U0,
                                                            const T* __restrict__ B, const T* __restrict__ Lin,
@@ -323,102 +432,8 @@ __global__ void __launch_bounds__(MW * MWPB) k_stage_march(Geom<T> g, Phys<T> p,
   if (threadIdx.x == 0) s_dt = step_dt<T>(g, rec, parity);
   __syncthreads();
   const double dt = s_dt;
-  const T tdt = (T)dt;
   StripGeom s;
-  if (strip_setup(g, SEG, s)) {
-    const int x = s.x;
-    const bool xin = x >= g.gc && x < g.gc + g.nx;
-    const int top = g.gc + g.ny;  // first top ghost row
-    // prologue: corner rows ys-2..ys+2, U1 rows ys-2..ys+1
-    const CornerRow<T> cm2 = load_corner_row(g, B, x, s.ys - 2);
-    const CornerRow<T> cm1 = load_corner_row(g, B, x, s.ys - 1);
-    CornerRow<T> c0 = load_corner_row(g, B, x, s.ys);
-    CornerRow<T> c1 = load_corner_row(g, B, x, s.ys + 1);
-    CornerRow<T> c2 = load_corner_row(g, B, x, s.ys + 2);
-    Cell3<T> u0c{(T)0, (T)0, (T)0}, u0n{(T)0, (T)0, (T)0}, dummy;
-    Cell3<T> uc = mirror_columns(g, s, stage1_row(g, p, tdt, U0, Lin, Sin, x, s.ys, xin, c0, c1, u0c), true);
-    Cell3<T> un;
-    if (s.ys + 1 >= top) {
-      un = mirror_row(uc);  // top ghost above a one-row segment
-    } else {
-      un = mirror_columns(g, s, stage1_row(g, p, tdt, U0, Lin, Sin, x, s.ys + 1, xin, c1, c2, u0n), true);
-    }
-    Cell3<T> um1, um2;
-    if (s.ys == g.gc) {  // bottom ghosts mirror rows gc, gc+1
-      um1 = mirror_row(uc);
-      um2 = mirror_row(un);
-    } else {
-      um1 = mirror_columns(g, s, stage1_row(g, p, tdt, U0, Lin, Sin, x, s.ys - 1, xin, cm1, c0, dummy), true);
-      um2 = mirror_columns(g, s, stage1_row(g, p, tdt, U0, Lin, Sin, x, s.ys - 2, xin, cm2, cm1, dummy), true);
-    }
-    // Ghost row top+1 mirrors row top-2, which leaves the window before it is needed.
-    Cell3<T> stash{(T)0, (T)0, (T)0};
-    if (s.ys + 1 == top) stash = mirror_row(um1);
-    YCarry<T> y;
-    {
-      Cell3<T> Lm, Rm, L0, R0;
-      const T blm = b_yface(g, cm1), b0 = b_yface(g, c0), b1 = b_yface(g, c1);
-      recon<T>(p, um2, um1, uc, blm, b0, Lm, Rm);
-      recon<T>(p, um1, uc, un, b0, b1, L0, R0);
-      T sp;
-      y.Gm = face<T, 1, false>(p, Rm, L0, sp);
-      y.R = R0;
-      y.Lh = L0.w;
-      y.Bl = b0;
-      y.Br = b1;
-    }
-    for (int j = s.ys; j < s.ye; ++j) {
-      // U1 of row j+2 (needs corner rows j+2, j+3)
-      const CornerRow<T> c3 = load_corner_row(g, B, x, j + 3);
-      Cell3<T> u2, u0x{(T)0, (T)0, (T)0};
-      if (j + 2 == top) {
-        u2 = mirror_row(un);   // row top mirrors top-1
-        stash = mirror_row(uc);  // row top+1 mirrors top-2
-      } else if (j + 2 == top + 1) {
-        u2 = stash;
-      } else {
-        u2 = mirror_columns(g, s, stage1_row(g, p, tdt, U0, Lin, Sin, x, j + 2, xin, c2, c3, u0x), j + 2 < top);
-      }
-      T sx;
-      Cell3<T> acc = x_derivative<T, false>(g, p, uc, c0, c1, sx);
-      Cell3<T> Ln, Rn;
-      const T b2 = b_yface(g, c2);
-      recon<T>(p, uc, un, u2, y.Br, b2, Ln, Rn);
-      T sp;
-      const Cell3<T> Gp = face<T, 1, false>(p, y.R, Ln, sp);
-      acc.w = acc.w - p.inv_dy * (Gp.w - y.Gm.w);
-      acc.hu = acc.hu - p.inv_dy * (Gp.hu - y.Gm.hu);
-      acc.hv = acc.hv - p.inv_dy * (Gp.hv - y.Gm.hv);
-      for (int b = 0; b < p.n_bottom; ++b)
-        acc.hv = acc.hv + p.neg_g * slope_over<T>(y.Br - y.Bl, p.dy, p.inv_dy, p.dy_pow2) * ((y.R.w + y.Lh) * (T)0.5);
-      acc.w = add_point_sources<T>(p, acc.w);
-      if (s.out_col) {
-        T w = uc.w + tdt * acc.w;
-        T hu = uc.hu + tdt * acc.hu;
-        T hv = uc.hv + tdt * acc.hv;
-        w = (T)0.5 * (u0c.w + w);
-        hu = (T)0.5 * (u0c.hu + hu);
-        hv = (T)0.5 * (u0c.hv + hv);
-        const T Bc = b_cell(g, c0, c1);
-        if (p.friction && friction_active<T>(uc.hu, uc.hv))
-          apply_friction<T>(tdt, friction_factor<T>(p, uc.w, uc.hu, uc.hv, Bc), hu, hv);
-        dry_clamp<T>(p, w, hu, hv, Bc);
-        store_with_ghosts<T>(g, Uo, x, j, w, hu, hv);
-      }
-      uc = un;
-      un = u2;
-      u0c = u0n;
-      u0n = u0x;
-      c0 = c1;
-      c1 = c2;
-      c2 = c3;
-      y.R = Rn;
-      y.Lh = Ln.w;
-      y.Bl = y.Br;
-      y.Br = b2;
-      y.Gm = Gp;
-    }
-  }
+  if (strip_setup(g, SEG, s)) stage_march_unit<T, false>(g, p, U0, B, Lin, Sin, Uo, s, (T)dt);
   if (root) advance_record<T>(rec, parity, dt);
 }
 

@@ -30,7 +30,10 @@ EXPORTED_SYMBOLS = (
     "vf_download_state", "vf_get_interior_state", "vf_step", "vf_simulate", "vf_water_volume",
     "vf_device_state", "vf_stream", "vf_time_steps", "vf_time_kernels", "vf_last_error", "vf_launch_count",
     "vf_water_volume_static",
+    "vf_batch_launch", "vf_batch_poll", "vf_batch_is_done", "vf_batch_collect", "vf_batch_wait", "vf_batch_free",
+    "vf_batch_simulate", "vf_batch_cluster_size", "vf_batch_last_error",
 )
+VF_BATCH_OK, VF_BATCH_TIMEOUT, VF_BATCH_STALLED, VF_BATCH_MAX_STEPS = 0, 1, 2, 3
 VF_STATIC_MAX_ROWS = 16384
 
 
@@ -52,6 +55,11 @@ class VfConfig(C.Structure):
         ("bottom_is_constant", C.c_int32), ("bottom_constant", C.c_double),
         ("device", C.c_int32),
     ]
+
+
+class VfBatchOptions(C.Structure):
+    _fields_ = [("tiles_per_cta", C.c_int32), ("max_cluster", C.c_int32), ("time_limit_s", C.c_double),
+                ("seg_rows", C.c_int32)]
 
 
 class NativeError(RuntimeError):
@@ -109,6 +117,19 @@ def load(build_if_missing: bool = False):
                                              C.c_double, C.c_double, C.c_int32, C.c_double, C.c_void_p,
                                              C.c_void_p]),
         "vf_launch_count": (C.c_int64, [H]),
+        "vf_batch_launch": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_double,
+                                      C.c_int64, C.POINTER(VfBatchOptions), C.POINTER(C.c_void_p)]),
+        "vf_batch_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
+        "vf_batch_is_done": (C.c_int, [C.c_void_p, C.c_int32]),
+        "vf_batch_collect": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
+        "vf_batch_wait": (C.c_int, [C.c_void_p]),
+        "vf_batch_free": (C.c_int, [C.c_void_p]),
+        "vf_batch_simulate": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_void_p, C.c_void_p, C.c_int32,
+                                        C.c_double, C.c_int64, C.POINTER(VfBatchOptions), C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p]),
+        "vf_batch_cluster_size": (C.c_int, [H, C.POINTER(VfBatchOptions), C.POINTER(C.c_int32)]),
+        "vf_batch_last_error": (C.c_char_p, [C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -121,6 +142,18 @@ def load(build_if_missing: bool = False):
 def check(lib, h, rc: int):
     if rc != VF_OK:
         msg = lib.vf_last_error(h)
+        text = msg.decode() if msg else ""
+        if rc == VF_EINVAL:
+            from .api import ArgumentError
+            raise ArgumentError(text)
+        if rc == VF_ENOMEM:
+            raise MemoryError(text)
+        raise NativeError(rc, text)
+
+
+def check_batch(lib, b, rc: int):
+    if rc != VF_OK:
+        msg = lib.vf_batch_last_error(b)
         text = msg.decode() if msg else ""
         if rc == VF_EINVAL:
             from .api import ArgumentError

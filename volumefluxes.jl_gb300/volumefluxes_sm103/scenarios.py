@@ -7,6 +7,18 @@
                        w = max(1.5, B_cell) (dry islands), Manning-type friction
                        n = 0.03 (friction_bsa2012, Cz = n^2), rain 1e-5 m/s,
                        infiltration 2e-6 m/s, wall BCs, RK2, CFL 0.25.
+  ensemble_member      one flood scenario of the batched ensemble: square side
+                       log-uniform in [64, 1024] cells with Δ = 1 m, 8-32 seeded
+                       hills (amplitude U[0.5,4] m, width U[50,400] m, centres in
+                       the domain) + 1e-3 * x, uniform initial depth U[0,2] m over
+                       the terrain (w = B_cell + h0), rain U[0,5e-5] m/s,
+                       Manning n U[0.01,0.08] (friction_bsa2012, Cz = n^2), wall
+                       BCs, RK2, CFL 0.25, end time U[10,600] s (rounded to a
+                       Float32 value, so Float32 time reaches it exactly), and
+                       depth_cutoff = 8e-2 as the reference's terrain example
+                       uses (examples/terrain.jl:92): with the default 1e-5, thin
+                       draining layers on the hill flanks drive the CFL step
+                       down to ~1e-5 s and a member needs millions of steps.
 
 Random numbers come from splitmix64 so any language can regenerate them.
 """
@@ -139,3 +151,50 @@ def hills_wet_dry(n: int = 4096, seed: int = 20240901, n_hills: int = 64, w_init
     return Scenario(name=f"hills_wet_dry_{n}", nx=n, ny=n, extent=extent, B=B, w0=w0, hu0=z, hv0=z.copy(), cfl=cfl,
                     rain_m_per_h=1e-5 * 3600, infiltration_m_per_s=2e-6, manning_n=0.03, bottom_source=True,
                     meta={"seed": seed, "n_hills": n_hills})
+
+
+ENSEMBLE_DEPTH_CUTOFF = 8e-2  # examples/terrain.jl:92
+
+
+@dataclass
+class EnsembleSpec:
+    """Draws of one ensemble member (everything but the arrays)."""
+    index: int
+    seed: int
+    side: int
+    n_hills: int
+    rain_m_per_s: float
+    manning_n: float
+    h0: float
+    endtime: float
+
+
+def ensemble_specs(count: int = 256, seed: int = 20241203, side_range=(64, 1024)) -> list[EnsembleSpec]:
+    """The seeded draws of `count` ensemble members (one splitmix64 stream)."""
+    rng = SplitMix64(seed)
+    lo, hi = np.log(side_range[0]), np.log(side_range[1])
+    out = []
+    for i in range(count):
+        side = int(round(float(np.exp(rng.uniform(lo, hi)))))
+        side = min(max(side, side_range[0]), side_range[1])
+        n_hills = 8 + min(24, int(rng.uniform(0.0, 25.0)))
+        rain = rng.uniform(0.0, 5e-5)
+        n = rng.uniform(0.01, 0.08)
+        h0 = rng.uniform(0.0, 2.0)
+        endtime = float(np.float32(rng.uniform(10.0, 600.0)))
+        out.append(EnsembleSpec(i, rng.next_u64(), side, n_hills, rain, n, h0, endtime))
+    return out
+
+
+def ensemble_member(spec: EnsembleSpec) -> Scenario:
+    n = spec.side
+    L = float(n)
+    extent = ((0.0, L), (0.0, L))
+    B = hill_bottom(n, n, extent, spec.n_hills, spec.seed, amp=(0.5, 4.0), width=(50.0, 400.0))
+    Bc = 0.25 * (B[:-1, :-1] + B[1:, :-1] + B[:-1, 1:] + B[1:, 1:])[2:-2, 2:-2]
+    w0 = Bc + spec.h0
+    z = np.zeros_like(w0)
+    return Scenario(name=f"ensemble_{spec.index}_{n}", nx=n, ny=n, extent=extent, B=B, w0=w0, hu0=z, hv0=z.copy(),
+                    cfl=0.25, rain_m_per_h=spec.rain_m_per_s * 3600, manning_n=spec.manning_n, bottom_source=True,
+                    eq={"depth_cutoff": ENSEMBLE_DEPTH_CUTOFF},
+                    meta={"seed": spec.seed, "n_hills": spec.n_hills, "endtime": spec.endtime, "h0": spec.h0})
