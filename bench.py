@@ -62,9 +62,13 @@ def parse():
                     help="seconds of oracle stepping the reference arm may spend (it runs min(K, budget) steps)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--ensemble-members", type=int, default=256)
-    ap.add_argument("--ensemble-plain-budget", type=float, default=40.0,
+    ap.add_argument("--ensemble-plain-budget", type=float, default=30.0,
                     help="seconds the sequential plain baseline of the ensemble may spend (it runs a sample)")
     ap.add_argument("--no-autotune", action="store_true", help="ensemble with the library's default granularity")
+    ap.add_argument("--serving", action="store_true", help="also measure the serving loop (adds ~2 min)")
+    ap.add_argument("--serving-requests", type=int, default=48)
+    ap.add_argument("--serving-rates", default="10,100,1000", help="Poisson arrival rates [req/s]")
+    ap.add_argument("--serving-budget-gb", type=float, default=120.0)
     return ap.parse_args()
 
 
@@ -420,6 +424,115 @@ def measure_ensemble(args, local):
                       "states resident on the device"}
 
 
+def serving_workload(n):
+    return (f"serving: {n} flood requests drawn as the ensemble members but with sides log-uniform in [128,2048], "
+            "Float32 or Float64 with probability 1/2, end times U[2,20] s; Poisson arrivals; HBM admission budget")
+
+
+def measure_serving(args, local):
+    """Continuous-batching server against a one-at-a-time plain server, same arrivals.
+
+    Served: requests are submitted at their Poisson arrival times to the
+    library's engine (vf_server_*: HBM-budget admission, one batch launch per
+    poll beside the running ones); a request's latency runs from its arrival to
+    the host holding its final state. Plain: one request at a time in arrival
+    order through the drop-in API (build/upload, simulate_to_time, download);
+    its service times are measured once back to back, and the FIFO latencies
+    of each arrival sequence follow exactly from them (finish = max(arrival,
+    previous finish) + service).
+    """
+    import volumefluxes_sm103 as vf
+    from volumefluxes_sm103 import scenarios as S
+    from volumefluxes_sm103.serving import Server
+    specs = S.serving_specs(args.serving_requests)
+    reqs = [(S.ensemble_member(r.spec), np.float32 if r.real == "f32" else np.float64, r.spec.endtime)
+            for r in specs]
+    rates = [float(x) for x in args.serving_rates.split(",") if x]
+    budget = int(args.serving_budget_gb * (1 << 30))
+    rng = np.random.default_rng(20241204)
+    gaps = rng.exponential(1.0, size=len(reqs))
+    work = sum(sc.nx * sc.ny for sc, _, _ in reqs)
+    out = {"workload": serving_workload(len(reqs)), "requests": len(reqs),
+           "f64_requests": sum(r == np.float64 for _, r, _ in reqs), "hbm_budget_bytes": budget, "rates": []}
+    # warm the kernels and the pool outside the timing
+    with Server(budget, device=local) as srv:
+        tk = [srv.submit(reqs[0][0], np.float32, 0.5), srv.submit(reqs[1][0], np.float64, 0.5)]
+        while len(tk):
+            for t in srv.poll():
+                srv.result(t)
+                tk.remove(t)
+            time.sleep(0.001)
+    ref_state = None
+    for rate in rates:
+        arrive = np.cumsum(gaps / rate)
+        arrive -= arrive[0]
+        lat = [None] * len(reqs)
+        with Server(budget, device=local) as srv:
+            t0 = time.perf_counter()
+            nxt = 0
+            ticket_of = {}
+            while any(l is None for l in lat):
+                now = time.perf_counter() - t0
+                while nxt < len(reqs) and arrive[nxt] <= now:
+                    sc, real, T = reqs[nxt]
+                    ticket_of[srv.submit(sc, real, T)] = nxt
+                    nxt += 1
+                for tk in srv.poll():
+                    i = ticket_of[tk]
+                    r = srv.result(tk)
+                    lat[i] = time.perf_counter() - t0 - arrive[i]
+                    if i == 0:
+                        st = r.state
+                        ref_state = st.h.copy() if ref_state is None else ref_state
+                        same0 = bool(np.array_equal(ref_state, st.h))
+                time.sleep(0.0002)
+            makespan = time.perf_counter() - t0
+            launches = srv.stats()["launches"]
+        lat = np.array(lat)
+        out["rates"].append({"rate_per_s": rate, "makespan_s": makespan, "throughput_req_per_s": len(reqs) / makespan,
+                             "latency_s": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
+                                           "p99": float(np.percentile(lat, 99))},
+                             "batch_launches": launches, "request0_same_as_first_rate": same0})
+    # one at a time through the drop-in API
+    service = []
+    for sc, real, T in reqs:
+        t1 = time.perf_counter()
+        sim = sc.build(vf.SM103Backend(real, device=local))
+        vf.simulate_to_time(sim, T)
+        st = vf.current_interior_state(sim)
+        sim.close()
+        service.append(time.perf_counter() - t1)
+    for row in out["rates"]:
+        rate = row["rate_per_s"]
+        arrive = np.cumsum(gaps / rate)
+        arrive -= arrive[0]
+        fin, lat = 0.0, []
+        for a, sv in zip(arrive, service):
+            fin = max(a, fin) + sv
+            lat.append(fin - a)
+        lat = np.array(lat)
+        row["plain_one_at_a_time"] = {"makespan_s": fin, "throughput_req_per_s": len(reqs) / fin,
+                                      "latency_s": {"p50": float(np.percentile(lat, 50)),
+                                                    "p95": float(np.percentile(lat, 95)),
+                                                    "p99": float(np.percentile(lat, 99))}}
+    # Float32 error against Float64 on the three smallest Float32 requests
+    small = sorted([i for i, (sc, r, _) in enumerate(reqs) if r == np.float32], key=lambda i: reqs[i][0].nx)[:3]
+    errs = []
+    for i in small:
+        sc, _, T = reqs[i]
+        a = sc.build(vf.SM103Backend(np.float32, device=local))
+        b = sc.build(vf.SM103Backend(np.float64, device=local))
+        vf.simulate_to_time(a, T)
+        vf.simulate_to_time(b, T)
+        errs.append(float(np.abs(vf.current_interior_state(a).h - vf.current_interior_state(b).h).max()))
+        a.close()
+        b.close()
+    out["f32_error_vs_f64"] = {"max_abs_w_m": max(errs), "members": [f"{reqs[i][0].nx}^2 to {reqs[i][2]:.2f} s"
+                                                                      for i in small]}
+    out["timing"] = "host wall clock; latency from arrival to the final interior state on the host"
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -465,9 +578,11 @@ def main():
         cpu = {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
                "sample": f"{steps} RK2 steps of the {sc.nx}x{sc.ny} Float64 workload from its initial state "
                          f"({el:.1f} s, OpenMP over rows)"}
-    ens = None
+    ens = serving = None
     if rank == 0 and world == 1 and not args.no_ensemble:
         ens = measure_ensemble(args, local)
+    if rank == 0 and world == 1 and args.serving:
+        serving = measure_serving(args, local)
     if rank != 0:
         return
     head = results[args.dtype]
@@ -483,6 +598,7 @@ def main():
         "cpu_baseline": cpu, "e2e": head["e2e"], "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
         "variants": {k: v for k, v in results.items() if k != args.dtype},
         "ensemble": ens,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
 

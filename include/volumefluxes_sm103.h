@@ -179,9 +179,12 @@ int vf_time_kernels(vf_handle* h, int64_t n_steps, float* ms_flux, float* ms_sta
  * One thread-block cluster per simulation runs its whole time loop on the
  * device; launches are grouped by cluster size (one launch per group,
  * concurrent streams), and the GPU's block scheduler starts a pending
- * simulation whenever a cluster finishes. Per-handle results are bitwise
- * those of vf_simulate on the same handle in Float64, and independent of
- * which other simulations share the launch in both precisions. */
+ * simulation whenever a cluster finishes. Simulations of at least wide_cells
+ * cells instead run the plain whole-grid kernels on their own stream, fed in
+ * CUDA-graph chunks by the host whenever the batch is polled or waited on.
+ * Per-handle results are bitwise those of vf_simulate on the same handle in
+ * Float64, and independent of which other simulations share the batch in both
+ * precisions. */
 #define VF_BATCH_OK 0          /* reached its end time */
 #define VF_BATCH_TIMEOUT 1     /* the launch's watchdog (time_limit_s) stopped it */
 #define VF_BATCH_STALLED 2     /* t + dt rounded to t: no progress possible */
@@ -193,6 +196,9 @@ typedef struct vf_batch_options {
   double time_limit_s;     /* watchdog from the batch's start, in seconds; <= 0: default (600 s) */
   int32_t seg_rows;        /* rows per strip segment of Float32 column-marching members
                               (8..256); 0: 64, halved down to 8 until every warp has two */
+  int64_t wide_cells;      /* members with at least this many interior cells run the plain
+                              whole-grid kernels on their own stream instead of a cluster;
+                              0: default (1048576), < 0: never */
 } vf_batch_options;
 
 typedef struct vf_batch vf_batch;
@@ -228,6 +234,42 @@ int vf_batch_simulate(vf_handle* const* hs, int32_t n, const double* t0, const d
 int vf_batch_cluster_size(vf_handle* h, const vf_batch_options* opt, int32_t* csize_out);
 /* Message for the last batch failure (b may be NULL for vf_batch_launch). */
 const char* vf_batch_last_error(vf_batch* b);
+
+/* ---- Serving ---------------------------------------------------------------
+ * A request loop over whole simulations (no counterpart in the reference).
+ * A request is a configuration, its bottom corners, an initial interior state,
+ * t0 and an end time; the engine keeps its state on the device from admission
+ * to completion and writes the final interior state to the caller's output
+ * buffers. Admission is oldest-first and bounded by an HBM budget (the device
+ * bytes vf_create allocates per request); every poll launches what it
+ * admitted as one batch beside the batches still running (continuous
+ * batching). Requests take SourceTermBottom, ConstantRain and
+ * ConstantInfiltration sources. Input buffers must stay valid until the
+ * request is admitted, output buffers until it is reported done. */
+typedef struct vf_server vf_server;
+
+/* opt: batch options of every launch (NULL: defaults); max_steps <= 0: none. */
+int vf_server_create(int32_t device, int64_t hbm_budget_bytes, const vf_batch_options* opt, int64_t max_steps,
+                     vf_server** out);
+/* Queues a request; *ticket_out identifies it. VF_ENOMEM if it alone exceeds the budget. */
+int vf_server_submit(vf_server* s, const vf_config* cfg, const void* B_corners, const void* w, const void* hu,
+                     const void* hv, double t0, double endtime, void* out_w, void* out_hu, void* out_hv,
+                     int64_t* ticket_out);
+/* Advances the engine (complete, admit, launch) without waiting on the GPU.
+ * Writes up to `capacity` tickets that finished during this call (done or
+ * failed) to done_tickets and their count to *n_done. */
+int vf_server_poll(vf_server* s, int64_t* done_tickets, int32_t capacity, int32_t* n_done);
+/* Outcome of a finished request: final time, steps, last dt, VF_BATCH_*
+ * status; returns the request's error code if it failed. */
+int vf_server_result(vf_server* s, int64_t ticket, double* t_out, int64_t* steps_out, double* last_dt_out,
+                     int32_t* status_out);
+/* Forgets a finished request. */
+int vf_server_release(vf_server* s, int64_t ticket);
+/* Device bytes charged to running requests, queue and running counts, batches launched. */
+int vf_server_stats(vf_server* s, int64_t* used_bytes, int32_t* queued, int32_t* running, int64_t* launches);
+/* Waits for running batches and frees everything. */
+int vf_server_destroy(vf_server* s);
+const char* vf_server_last_error(vf_server* s);
 
 /* Largest interior row count vf_water_volume_static accepts. */
 #define VF_STATIC_MAX_ROWS 16384

@@ -105,3 +105,23 @@ def test_batch_rejects_bad_arguments_without_touching_the_gpu(lib):
     assert not b.value
     assert lib.vf_batch_poll(None, None) == N.VF_EINVAL
     assert lib.vf_batch_free(None) == N.VF_OK
+
+
+def test_server_rejects_requests_without_touching_the_gpu(lib):
+    s = ctypes.c_void_p()
+    assert lib.vf_server_create(0, 0, None, 0, ctypes.byref(s)) == N.VF_EINVAL
+    assert lib.vf_server_create(0, 1 << 20, None, 0, ctypes.byref(s)) == N.VF_OK
+    import numpy as np
+    w = np.zeros((16, 16))
+    tk = ctypes.c_int64()
+    big = _cfg(nx=1024, ny=1024)
+    rc = lib.vf_server_submit(s, ctypes.byref(big), None, w.ctypes.data, w.ctypes.data, w.ctypes.data, 0.0, 1.0,
+                              None, None, None, ctypes.byref(tk))
+    assert rc == N.VF_ENOMEM and b"budget" in lib.vf_server_last_error(s)
+    tab = _cfg(n_sources=1)
+    tab.source_kind[0] = N.VF_SRC_TIME_RAIN
+    rc = lib.vf_server_submit(s, ctypes.byref(tab), None, w.ctypes.data, w.ctypes.data, w.ctypes.data, 0.0, 1.0,
+                              None, None, None, ctypes.byref(tk))
+    assert rc == N.VF_EINVAL
+    assert lib.vf_server_result(s, 12345, None, None, None, None) == N.VF_EINVAL
+    assert lib.vf_server_destroy(s) == N.VF_OK

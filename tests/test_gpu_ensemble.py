@@ -160,3 +160,41 @@ def test_batch_rejects_duplicates_and_unready_handles():
     sim = sc.build(vf.SM103Backend())
     with pytest.raises(vf.ArgumentError):
         E.simulate_batch([sim, sim], 1.0)
+
+
+@pytest.mark.parametrize("real", [np.float64, np.float32])
+def test_wide_members_match_narrow_members_and_the_plain_loop(real):
+    """Members above wide_cells run the whole-grid kernels fed in graph chunks,
+    so they end bit for bit where the plain loop ends. In Float64 the cluster
+    path agrees bit for bit too; in Float32 (multiply-add contraction decided
+    per kernel) it agrees to rounding."""
+    scen = [hills_rect(200, 150), hills_rect(64, 48), hills_rect(130, 70, stepper="fe")]
+    T = 3.0
+    wide = [sc.build(vf.SM103Backend(real)) for sc in scen]
+    rw = E.simulate_batch(wide, T, options=E.BatchOptions(wide_cells=9000))  # the first and third go wide
+    narrow = [sc.build(vf.SM103Backend(real)) for sc in scen]
+    rn = E.simulate_batch(narrow, T, options=E.BatchOptions(wide_cells=-1))
+    for k, (sc, a, b, x, y) in enumerate(zip(scen, wide, narrow, rw, rn)):
+        assert x.status == y.status == N.VF_BATCH_OK and x.t == y.t == T
+        plain = sc.build(vf.SM103Backend(real))
+        vf.simulate_to_time(plain, T)
+        assert plain.t == x.t
+        if k != 1 or real == np.float64:  # wide (or Float64): the plain loop's kernels
+            assert_bitwise(vf.current_interior_state(a), interior(plain))
+        if real == np.float64:
+            assert (x.steps, x.last_dt) == (y.steps, y.last_dt)
+            assert_bitwise(vf.current_interior_state(a), interior(b))
+        else:
+            d = np.abs(vf.current_interior_state(a).h - vf.current_interior_state(b).h).max()
+            assert d <= 1e-3, d
+
+
+def test_wide_member_max_steps_is_exact():
+    sc = hills_rect(200, 150)
+    sim = sc.build(vf.SM103Backend())
+    (r,) = E.simulate_batch([sim], 100.0, max_steps=37, options=E.BatchOptions(wide_cells=1))
+    assert r.status == N.VF_BATCH_MAX_STEPS and r.steps == 37
+    other = sc.build(vf.SM103Backend())
+    (q,) = E.simulate_batch([other], 100.0, max_steps=37, options=E.BatchOptions(wide_cells=-1))
+    assert (q.steps, q.t) == (37, r.t)
+    assert_bitwise(vf.current_interior_state(sim), interior(other))

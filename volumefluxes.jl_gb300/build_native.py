@@ -1,6 +1,6 @@
 """Build libvfsm103.so, the sm_103a shallow-water step library, in-tree.
 
-Five translation units compile in parallel with nvcc and link into one shared
+Six translation units compile in parallel with nvcc and link into one shared
 library with the CUDA runtime linked statically:
 
   vf_f64.cu  Float64 kernels, -fmad=false (each operation rounds as in Julia)
@@ -8,6 +8,7 @@ library with the CUDA runtime linked statically:
   vf_abi.cu  the extern "C" boundary of include/volumefluxes_sm103.h
   vf_noalloc.cu  the allocation-free water-volume entry point
   vf_batch.cu  the batched-ensemble entry points
+  vf_server.cu  the serving engine
 
 Usage: python volumefluxes.jl_gb300/build_native.py [--force]
 """
@@ -35,6 +36,7 @@ UNITS = {
     "vf_abi.cu": [],
     "vf_noalloc.cu": [],
     "vf_batch.cu": [],
+    "vf_server.cu": [],
 }
 
 

@@ -186,6 +186,7 @@ void refresh_params(vf_handle* h) {
   fill_phys(h, h->ad.p);
   fill_phys(h, h->af.p);
   select_variants(h);
+  h->chunk_k = 0;  // a captured step chunk holds the old parameters
 }
 
 int validate(const vf_config* c) {
@@ -317,6 +318,7 @@ void destroy(vf_handle* h) {
     cudaStreamSynchronize(h->stream);
     cudaStreamDestroy(h->stream);
   }
+  if (h->chunk_exec) cudaGraphExecDestroy(h->chunk_exec);
   delete h->rec_h;
   delete h;
 }
@@ -325,6 +327,66 @@ void destroy(vf_handle* h) {
 
 namespace vf {
 int handle_ready(vf_handle* h) { return ensure_ready(h); }
+
+int handle_begin_loop(vf_handle* h, double t0, double endtime, int match_endtime, double maximum_timestep) {
+  reset_record(h);
+  vf::StepRecord* r = h->rec_h;
+  r->t[0] = t0;
+  r->active[0] = t0 < endtime ? 1 : 0;
+  r->match_endtime = match_endtime ? 1 : 0;
+  r->has_max_ts = maximum_timestep >= 0 ? 1 : 0;
+  r->max_ts = maximum_timestep;
+  r->endtime = endtime;
+  return push_record(h);
+}
+
+int handle_enqueue_steps(vf_handle* h, long long first, int n) {
+  for (int i = 0; i < n; ++i)
+    if (int rc = launch_one_step(h, (int)((first + i) & 1))) return rc;
+  return VF_OK;
+}
+
+int handle_enqueue_chunk(vf_handle* h, int k) {
+  if (!h->chunk_exec || h->chunk_k != k || h->chunk_u0 != h->U[0]) {
+    if (h->chunk_exec) {
+      cudaGraphExecDestroy(h->chunk_exec);
+      h->chunk_exec = nullptr;
+    }
+    VF_CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = h->launches;
+    int rc = handle_enqueue_steps(h, 0, k);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+    h->launches = before;
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(h, e, "step chunk capture");
+    e = cudaGraphInstantiate(&h->chunk_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      h->chunk_exec = nullptr;
+      return cuda_fail(h, e, "step chunk instantiation");
+    }
+    h->chunk_k = k;
+    h->chunk_u0 = h->U[0];
+  }
+  VF_CK(h, cudaGraphLaunch(h->chunk_exec, h->stream));
+  h->launches += 2LL * k;
+  return VF_OK;
+}
+
+size_t handle_device_bytes(const vf_config* c) {
+  const long long N1 = c->nx + 2LL * c->gc, N2 = c->ny + 2LL * c->gc;
+  const long long P = round_up(vf::XOFF + N1, 32), PS = P * N2, PB = round_up(vf::XOFF + N1 + 1, 32);
+  const size_t e = (size_t)c->real_bytes;
+  size_t b = 3 * (size_t)(3 * PS) * e;                    // U[0], U[1], L
+  if (c->friction != VF_FRICTION_NONE) b += (size_t)PS * e;
+  if (!c->bottom_is_constant) b += (size_t)(PB * (N2 + 1)) * e;
+  b += sizeof(vf::StepRecord) + sizeof(double) * 1025;    // record, volume partials and result
+  return b;
+}
 }  // namespace vf
 
 extern "C" {

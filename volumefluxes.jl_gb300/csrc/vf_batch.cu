@@ -9,13 +9,25 @@
 // the block scheduler then starts in that order (longest-processing-time
 // first). Each cluster writes its result and a done flag into pinned, mapped
 // host memory, so the host sees every simulation finish without synchronising
-// the launch it belongs to. Nothing here allocates with cudaMalloc, cudaFree
-// or cudaFreeHost, which may synchronise the whole device: launch descriptors
-// come from the library's stream-ordered pool and result slots from a pinned
-// slab kept for the life of the process.
+// the launch it belongs to.
+//
+// Simulations of at least wide_cells interior cells are "wide": a 16-CTA
+// cluster would leave most of the GPU to them alone, so they run the plain
+// whole-grid step kernels on their handle's stream instead, as the device loop
+// of vf_simulate, in chunks of kChunk steps captured once as a CUDA graph. Two
+// chunks are kept in flight; after each, the step record is copied to pinned
+// memory behind an event, and the host retires chunks and enqueues new ones
+// whenever the batch is polled. Their kernels share the SMs with the cluster
+// launches, and their results are those of vf_simulate.
+//
+// Nothing here allocates with cudaMalloc, cudaFree or cudaFreeHost, which may
+// synchronise the whole device: launch descriptors come from the library's
+// stream-ordered pool and result slots from a pinned slab kept for the life of
+// the process.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstring>
@@ -26,9 +38,26 @@
 
 #include "vf_handle.h"
 
+namespace {
+// A wide member: the plain device loop on its handle's stream, fed in chunks.
+struct Wide {
+  int member = 0;
+  long long enqueued = 0;      // steps enqueued so far
+  long long max_steps = 0;
+  int head = 0, inflight = 0;  // chunks head .. head+inflight-1 are in flight; chunk c uses ev/rec slot c & 1
+  long long chunk_end[2] = {0, 0};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  double last_t = 0;
+  bool done = false;
+};
+}  // namespace
+
 struct vf_batch {
   int device = 0;
   int n = 0;
+  std::vector<Wide> wide;
+  std::chrono::steady_clock::time_point start;
+  double time_limit_s = 0;
   std::vector<vf_handle*> hs;
   std::vector<cudaStream_t> streams;
   std::vector<int> slots;          // result slot of simulation i
@@ -51,17 +80,24 @@ int bfail(vf_batch* b, int code, const std::string& msg) {
 }
 
 // ---- result slots: pinned, device-mapped, never freed ---------------------
+// A slot holds the result a cluster writes (res) and, for wide members, the
+// two step-record copies of the chunks in flight.
+struct Slot {
+  vf::EnsResult res;
+  vf::StepRecord rec[2];
+};
+
 constexpr int kSlab = 4096;
 std::mutex g_slot_mu;
-std::vector<vf::EnsResult*> g_slabs;  // host pointers
-std::vector<vf::EnsResult*> g_slabs_d;
+std::vector<Slot*> g_slabs;  // host pointers
+std::vector<Slot*> g_slabs_d;
 std::vector<int> g_free_slots;
 
 int acquire_slots(int n, std::vector<int>& out, std::string& err) {
   std::lock_guard<std::mutex> lk(g_slot_mu);
   while ((int)g_free_slots.size() < n) {
     void* p = nullptr;
-    if (cudaHostAlloc(&p, sizeof(vf::EnsResult) * kSlab, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess) {
+    if (cudaHostAlloc(&p, sizeof(Slot) * kSlab, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess) {
       cudaGetLastError();
       err = "pinned result slab allocation failed";
       return VF_ENOMEM;
@@ -73,8 +109,8 @@ int acquire_slots(int n, std::vector<int>& out, std::string& err) {
       return VF_ECUDA;
     }
     const int base = (int)g_slabs.size() * kSlab;
-    g_slabs.push_back(static_cast<vf::EnsResult*>(p));
-    g_slabs_d.push_back(static_cast<vf::EnsResult*>(d));
+    g_slabs.push_back(static_cast<Slot*>(p));
+    g_slabs_d.push_back(static_cast<Slot*>(d));
     for (int i = kSlab - 1; i >= 0; --i) g_free_slots.push_back(base + i);
   }
   out.resize(n);
@@ -90,8 +126,9 @@ void release_slots(const std::vector<int>& s) {
   for (int v : s) g_free_slots.push_back(v);
 }
 
-vf::EnsResult* slot_host(int s) { return g_slabs[s / kSlab] + s % kSlab; }
-vf::EnsResult* slot_dev(int s) { return g_slabs_d[s / kSlab] + s % kSlab; }
+vf::EnsResult* slot_host(int s) { return &(g_slabs[s / kSlab] + s % kSlab)->res; }
+vf::EnsResult* slot_dev(int s) { return &(g_slabs_d[s / kSlab] + s % kSlab)->res; }
+vf::StepRecord* slot_rec(int s, int k) { return &(g_slabs[s / kSlab] + s % kSlab)->rec[k]; }
 
 int slot_done(int s) { return __atomic_load_n(&slot_host(s)->done, __ATOMIC_ACQUIRE); }
 
@@ -101,11 +138,14 @@ struct Opts {
   int max_cluster;
   double time_limit_s;
   int seg_rows;  // 0: heuristic
+  long long wide_cells;
 };
 
 Opts resolve(const vf_batch_options* o) {
-  Opts r{16, 16, 600.0, 0};
+  Opts r{16, 16, 600.0, 0, 1LL << 20};
   if (o) {
+    if (o->wide_cells > 0) r.wide_cells = o->wide_cells;
+    if (o->wide_cells < 0) r.wide_cells = LLONG_MAX;
     if (o->tiles_per_cta > 0) r.tiles_per_cta = o->tiles_per_cta;
     if (o->max_cluster > 0) r.max_cluster = std::min(16, o->max_cluster);
     if (o->time_limit_s > 0) r.time_limit_s = o->time_limit_s;
@@ -114,14 +154,18 @@ Opts resolve(const vf_batch_options* o) {
   return r;
 }
 
-// Kernel design of a member: column marching (0) for Float32 members with wall
-// BCs, linear reconstruction, constant sources and RK2 (as the plain path
-// chooses, vf_abi.cu select_variants); tiles (1) for everything else.
-int variant_of(const vf_handle* h) { return h->elem == 4 && h->af.variant == 0 && h->af.rk2 ? 0 : 1; }
+// Kernel design of a member, as the plain path chooses it (vf_abi.cu
+// select_variants): column marching for Float32 members with wall BCs, linear
+// reconstruction and constant sources (0 with RK2, 2 with forward Euler);
+// tiles (1) for everything else.
+int variant_of(const vf_handle* h) {
+  if (h->elem == 4 && h->af.variant == 0) return h->af.rk2 ? 0 : 2;
+  return 1;
+}
 
 // Largest launchable cluster size <= c on the current device.
 std::mutex g_fit_mu;
-int g_fit[64][2][2][17];  // [device][precision][variant][c]: 0 unknown, else 1 + launchable
+int g_fit[64][2][3][17];  // [device][precision][variant][c]: 0 unknown, else 1 + launchable
 
 int fit_cluster(int device, int real_bytes, int variant, int c) {
   const int pi = real_bytes == 8 ? 0 : 1;
@@ -196,8 +240,90 @@ void destroy_batch(vf_batch* b) {
     cudaFreeAsync(b->epoch_d, b->setup);
   }
   for (cudaStream_t s : b->streams) cudaStreamDestroy(s);
+  for (Wide& w : b->wide)
+    for (cudaEvent_t e : w.ev)
+      if (e) cudaEventDestroy(e);
   release_slots(b->slots);
   delete b;
+}
+
+constexpr int kChunk = 16;  // steps per graph launch of a wide member
+
+// Final result of a wide member from the record copy of its last retired chunk.
+void wide_finish(vf_batch* b, Wide& w, const vf::StepRecord& r, long long k, int status) {
+  vf_handle* h = b->hs[w.member];
+  cudaStreamSynchronize(h->stream);  // no-op steps of a chunk still in flight
+  vf::EnsResult* res = slot_host(b->slots[w.member]);
+  res->t = r.t[k & 1];
+  res->last_dt = r.last_dt;
+  res->steps = r.n_done;
+  res->status = status;
+  w.done = true;
+  __atomic_store_n(&res->done, 1, __ATOMIC_RELEASE);
+}
+
+int wide_enqueue(vf_batch* b, Wide& w) {
+  vf_handle* h = b->hs[w.member];
+  const long long left = w.max_steps - w.enqueued;
+  const int n = (int)std::min<long long>(kChunk, left);
+  int rc = (n == kChunk && (w.enqueued & 1) == 0) ? vf::handle_enqueue_chunk(h, kChunk)
+                                                  : vf::handle_enqueue_steps(h, w.enqueued, n);
+  if (rc) return rc;
+  w.enqueued += n;
+  const int slot = (w.head + w.inflight) & 1;
+  cudaError_t e = cudaMemcpyAsync(slot_rec(b->slots[w.member], slot), h->rec, sizeof(vf::StepRecord),
+                                  cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(w.ev[slot], h->stream);
+  if (e != cudaSuccess) return VF_ECUDA;
+  w.chunk_end[slot] = w.enqueued;
+  w.inflight += 1;
+  return VF_OK;
+}
+
+// Retire finished chunks of every wide member and keep two in flight.
+int pump(vf_batch* b) {
+  if (b->wide.empty()) return VF_OK;
+  const double elapsed =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - b->start).count();
+  const bool late = elapsed > b->time_limit_s;
+  for (Wide& w : b->wide) {
+    if (w.done) continue;
+    while (w.inflight > 0) {
+      const int slot = w.head & 1;
+      const cudaError_t q = cudaEventQuery(w.ev[slot]);
+      if (q == cudaErrorNotReady) break;
+      if (q != cudaSuccess) return bfail(b, VF_ECUDA, std::string("wide member: ") + cudaGetErrorString(q));
+      const vf::StepRecord& r = *slot_rec(b->slots[w.member], slot);
+      const long long k = w.chunk_end[slot];
+      w.head += 1;
+      w.inflight -= 1;
+      if (!r.active[k & 1]) {
+        wide_finish(b, w, r, k, vf::kEnsOk);
+        break;
+      }
+      if (k >= w.max_steps) {
+        wide_finish(b, w, r, k, vf::kEnsMaxSteps);
+        break;
+      }
+      if (r.t[k & 1] == w.last_t && k > 0) {  // a whole chunk without progress
+        wide_finish(b, w, r, k, vf::kEnsStalled);
+        break;
+      }
+      w.last_t = r.t[k & 1];
+      if (late && w.inflight == 0) {
+        wide_finish(b, w, r, k, vf::kEnsTimeout);
+        break;
+      }
+    }
+    if (!w.done && late && w.inflight == 0) {
+      const int last = (w.head - 1) & 1;
+      wide_finish(b, w, *slot_rec(b->slots[w.member], last), w.chunk_end[last], vf::kEnsTimeout);
+    }
+    if (w.done || late) continue;
+    while (w.inflight < 2 && w.enqueued < w.max_steps)
+      if (int rc = wide_enqueue(b, w)) return bfail(b, rc, "wide member launch: " + b->hs[w.member]->err);
+  }
+  return VF_OK;
 }
 
 struct Group {
@@ -240,11 +366,22 @@ int vf_batch_launch(vf_handle* const* hs, int32_t n, const double* t0, const dou
   }
   for (int i = 0; i < n; ++i) std::memset(slot_host(b->slots[i]), 0, sizeof(vf::EnsResult));
 
-  // Groups by precision and cluster size; inside a group, largest work first.
+  b->start = std::chrono::steady_clock::now();
+  b->time_limit_s = o.time_limit_s;
+  // Wide members apart; the rest in groups by precision, kernel design and
+  // cluster size, largest work first inside a group.
   std::vector<Group> groups;
   std::vector<double> work(n);
   for (int i = 0; i < n; ++i) {
     const vf_handle* h = hs[i];
+    if ((long long)h->cfg.nx * h->cfg.ny >= o.wide_cells) {
+      Wide w;
+      w.member = i;
+      w.max_steps = max_steps > 0 ? max_steps : LLONG_MAX;
+      w.last_t = t0[i];
+      b->wide.push_back(w);
+      continue;
+    }
     const int prec = h->elem == 8 ? 0 : 1;
     const int var = variant_of(h);
     const int c = fit_cluster(device, (int)h->elem, var, cluster_for(h, o));
@@ -262,10 +399,32 @@ int vf_batch_launch(vf_handle* const* hs, int32_t n, const double* t0, const dou
     std::stable_sort(g.members.begin(), g.members.end(), [&](int a, int c) { return work[a] > work[c]; });
   std::stable_sort(groups.begin(), groups.end(), [](const Group& a, const Group& c) { return a.csize > c.csize; });
 
+  // Wide members start first: their first two chunks go in before any cluster.
+  for (Wide& w : b->wide) {
+    vf_handle* h = hs[w.member];
+    bool ok = cudaEventCreateWithFlags(&w.ev[0], cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&w.ev[1], cudaEventDisableTiming) == cudaSuccess;
+    int rc = ok ? vf::handle_begin_loop(h, t0[w.member], endtime[w.member], match_endtime, maximum_timestep)
+                : VF_ECUDA;
+    for (int k = 0; rc == VF_OK && k < 2 && w.enqueued < w.max_steps; ++k) rc = wide_enqueue(b, w);
+    if (rc) {
+      cudaGetLastError();
+      for (Wide& x : b->wide) cudaStreamSynchronize(hs[x.member]->stream);
+      const std::string msg = std::string("wide member start: ") + h->err;
+      destroy_batch(b);
+      return bfail(nullptr, rc ? rc : VF_ECUDA, msg);
+    }
+  }
+  if (groups.empty()) {
+    *out = b;
+    return VF_OK;
+  }
+
   for (size_t g = 0; g < groups.size(); ++g) {
     cudaStream_t s = nullptr;
     if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
       cudaGetLastError();
+      for (Wide& x : b->wide) cudaStreamSynchronize(hs[x.member]->stream);
       destroy_batch(b);
       return bfail(nullptr, VF_ECUDA, "stream creation failed");
     }
@@ -279,6 +438,7 @@ int vf_batch_launch(vf_handle* const* hs, int32_t n, const double* t0, const dou
   if (e == cudaSuccess) e = cudaMemsetAsync(b->epoch_d, 0, sizeof(unsigned long long), b->setup);
   if (e != cudaSuccess) {
     cudaGetLastError();
+    for (Wide& x : b->wide) cudaStreamSynchronize(hs[x.member]->stream);
     destroy_batch(b);
     return bfail(nullptr, VF_ENOMEM, "batch scratch allocation failed");
   }
@@ -324,6 +484,7 @@ int vf_batch_launch(vf_handle* const* hs, int32_t n, const double* t0, const dou
   if (e == cudaSuccess) e = cudaStreamSynchronize(b->setup);
   if (e != cudaSuccess) {
     cudaGetLastError();
+    for (Wide& x : b->wide) cudaStreamSynchronize(hs[x.member]->stream);
     destroy_batch(b);
     return bfail(nullptr, VF_ECUDA, std::string("batch descriptors: ") + cudaGetErrorString(e));
   }
@@ -340,6 +501,7 @@ int vf_batch_launch(vf_handle* const* hs, int32_t n, const double* t0, const dou
       cudaGetLastError();
       // Launches already issued run to completion before anything is freed.
       for (size_t k = 0; k < g; ++k) cudaStreamSynchronize(b->streams[k]);
+      for (Wide& x : b->wide) cudaStreamSynchronize(hs[x.member]->stream);
       destroy_batch(b);
       return bfail(nullptr, VF_ECUDA, std::string("ensemble launch: ") + cudaGetErrorString(e));
     }
@@ -351,6 +513,7 @@ int vf_batch_launch(vf_handle* const* hs, int32_t n, const double* t0, const dou
 
 int vf_batch_poll(vf_batch* b, int32_t* n_done) {
   if (!b || !n_done) return bfail(b, VF_EINVAL, "NULL argument");
+  if (int rc = pump(b)) return rc;
   int c = 0;
   for (int i = 0; i < b->n; ++i) c += slot_done(b->slots[i]) ? 1 : 0;
   *n_done = c;
@@ -359,6 +522,7 @@ int vf_batch_poll(vf_batch* b, int32_t* n_done) {
 
 int vf_batch_is_done(vf_batch* b, int32_t i) {
   if (!b || i < 0 || i >= b->n) return bfail(b, VF_EINVAL, "bad batch index");
+  if (int rc = pump(b)) return rc;
   return slot_done(b->slots[i]) ? 1 : 0;
 }
 
@@ -381,6 +545,17 @@ int vf_batch_collect(vf_batch* b, int32_t i, double* t_out, int64_t* steps_out, 
 int vf_batch_wait(vf_batch* b) {
   if (!b) return bfail(b, VF_EINVAL, "NULL batch");
   if (cudaSetDevice(b->device) != cudaSuccess) return bfail(b, VF_ECUDA, "cudaSetDevice failed");
+  for (;;) {  // wide members need the host to feed them
+    if (int rc = pump(b)) return rc;
+    bool all = true;
+    for (const Wide& w : b->wide) all = all && w.done;
+    if (all) break;
+    for (Wide& w : b->wide)
+      if (!w.done && w.inflight > 0) {
+        cudaEventSynchronize(w.ev[w.head & 1]);
+        break;
+      }
+  }
   for (cudaStream_t s : b->streams) {
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return bfail(b, VF_ECUDA, std::string("ensemble: ") + cudaGetErrorString(e));

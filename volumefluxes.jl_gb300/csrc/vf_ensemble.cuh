@@ -112,11 +112,14 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // fill the shared memory (2 x 77 KB); Float32 takes three.
 template <typename T> struct EnsBlocks { static constexpr int value = sizeof(T) == 8 ? 2 : 3; };
 
-// VAR 0: column-marching phases (vf_march.cuh), each warp taking strip
+// VAR 0: column-marching RK2 phases (vf_march.cuh), each warp taking strip
 // segments (strip, seg) = unit % nstrips, unit / nstrips, for units
 // rank * 8 + warp, stepping by 8 * C; wall BCs, linear reconstruction and
-// constant sources only. VAR 1: shared-memory tile phases (vf_kernels.cuh),
-// every configuration.
+// constant sources only -- the kernels the plain path runs for such Float32
+// simulations. VAR 2: the same flux phase with the forward-Euler update per
+// tile. VAR 1: shared-memory tile phases (vf_kernels.cuh), every
+// configuration. Each variant is its own kernel so that one's code does not
+// change how another is compiled.
 template <typename T, int VAR>
 __global__ void __launch_bounds__(NT, EnsBlocks<T>::value) k_ensemble(const EnsItem<T>* __restrict__ items,
                                                                       const int* __restrict__ order, int csize,
@@ -167,7 +170,7 @@ __global__ void __launch_bounds__(NT, EnsBlocks<T>::value) k_ensemble(const EnsI
     const T* U0 = sit.U[n & 1];
     T* U1 = sit.U[(n & 1) ^ 1];
     unsigned long long kx = 0, ky = 0;
-    if constexpr (VAR == 0) {
+    if constexpr (VAR != 1) {
       unsigned long long mx = 0, my = 0;
       for (int u = (int)rank * kWarps + warp; u < nunits; u += csize * kWarps) {
         StripGeom s;
@@ -212,6 +215,10 @@ __global__ void __launch_bounds__(NT, EnsBlocks<T>::value) k_ensemble(const EnsI
         strip_setup_at(g, seg, u % nstrips, u / nstrips, s);
         stage_march_unit<T, true>(g, p, U0, sit.B, sit.L, sit.S, U1, s, (T)dt);
       }
+    } else if constexpr (VAR == 2) {
+      for (int tile = (int)rank; tile < ntiles; tile += csize)
+        apply_fe_tile<T, true>(g, p, U0, sit.B, sit.L, sit.S, U1, g.gc + (tile % tiles_x) * TX,
+                               g.gc + (tile / tiles_x) * TY, dt);
     } else {
       for (int tile = (int)rank; tile < ntiles; tile += csize) {
         const int x0 = g.gc + (tile % tiles_x) * TX, y0 = g.gc + (tile / tiles_x) * TY;

@@ -31,18 +31,19 @@ cudaError_t configure_impl() {
   e = cudaFuncSetAttribute(k_ensemble<T, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if constexpr (sizeof(T) == 4) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ensemble<T, 0>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_ensemble<T, 2>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   }
   return e;
 }
 
-// Column marching (variant 0) exists for Float32 only: the Float64 members
-// run on tiles, where full warps keep the 1/64-rate FP64 pipe busy.
+// Column marching (variants 0 and 2) exists for Float32 only: the Float64
+// members run on tiles, where full warps keep the 1/64-rate FP64 pipe busy.
 template <typename T, int VAR>
 cudaLaunchConfig_t ensemble_config(int n, int csize, cudaStream_t st, cudaLaunchAttribute* attr) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(n * csize), 1, 1);
   cfg.blockDim = dim3(NT, 1, 1);
-  cfg.dynamicSmemBytes = VAR == 1 ? sizeof(SmemEns<T>) : 0;
+  cfg.dynamicSmemBytes = VAR == 1 ? sizeof(SmemEns<T>) : 0;  // marching needs none
   cfg.stream = st;
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = (unsigned)csize;
@@ -57,11 +58,12 @@ template <typename T>
 cudaError_t launch_ensemble_impl(const EnsItem<T>* items, const int* order, int n, int csize, int variant,
                                  unsigned long long time_limit_ns, cudaStream_t st) {
   cudaLaunchAttribute attr[1];
-  if (variant == 0) {
+  if (variant == 0 || variant == 2) {
     if constexpr (sizeof(T) == 8) {
       return cudaErrorInvalidValue;
     } else {
       cudaLaunchConfig_t cfg = ensemble_config<T, 0>(n, csize, st, attr);
+      if (variant == 2) return cudaLaunchKernelEx(&cfg, k_ensemble<T, 2>, items, order, csize, time_limit_ns);
       return cudaLaunchKernelEx(&cfg, k_ensemble<T, 0>, items, order, csize, time_limit_ns);
     }
   }
@@ -72,11 +74,12 @@ cudaError_t launch_ensemble_impl(const EnsItem<T>* items, const int* order, int 
 template <typename T>
 cudaError_t ensemble_max_clusters_impl(int csize, int variant, int* out) {
   cudaLaunchAttribute attr[1];
-  if (variant == 0) {
+  if (variant == 0 || variant == 2) {
     if constexpr (sizeof(T) == 8) {
       return cudaErrorInvalidValue;
     } else {
       cudaLaunchConfig_t cfg = ensemble_config<T, 0>(1, csize, nullptr, attr);
+      if (variant == 2) return cudaOccupancyMaxActiveClusters(out, k_ensemble<T, 2>, &cfg);
       return cudaOccupancyMaxActiveClusters(out, k_ensemble<T, 0>, &cfg);
     }
   }

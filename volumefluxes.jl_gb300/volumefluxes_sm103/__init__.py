@@ -18,7 +18,7 @@ from .api import (  # noqa: F401
     friction_bsa2012, friction_fcg2016, friction_bh2021, ImplicitFriction,
     TimeStepper, RungeKutta2, ForwardEulerStepper, number_of_substeps,
     SM103Backend, name, get_available_backends, convert_to_backend,
-    System, ConservedSystem, StateView, Simulator,
+    System, ConservedSystem, StateView, Simulator, system_config,
     set_current_state, current_state, current_interior_state, current_time, current_timestep,
     perform_step, water_volume, simulate_to_time, IntervalWriter, MultipleCallbacks,
 )

@@ -32,6 +32,8 @@ EXPORTED_SYMBOLS = (
     "vf_water_volume_static",
     "vf_batch_launch", "vf_batch_poll", "vf_batch_is_done", "vf_batch_collect", "vf_batch_wait", "vf_batch_free",
     "vf_batch_simulate", "vf_batch_cluster_size", "vf_batch_last_error",
+    "vf_server_create", "vf_server_submit", "vf_server_poll", "vf_server_result", "vf_server_release",
+    "vf_server_stats", "vf_server_destroy", "vf_server_last_error",
 )
 VF_BATCH_OK, VF_BATCH_TIMEOUT, VF_BATCH_STALLED, VF_BATCH_MAX_STEPS = 0, 1, 2, 3
 VF_STATIC_MAX_ROWS = 16384
@@ -59,7 +61,7 @@ class VfConfig(C.Structure):
 
 class VfBatchOptions(C.Structure):
     _fields_ = [("tiles_per_cta", C.c_int32), ("max_cluster", C.c_int32), ("time_limit_s", C.c_double),
-                ("seg_rows", C.c_int32)]
+                ("seg_rows", C.c_int32), ("wide_cells", C.c_int64)]
 
 
 class NativeError(RuntimeError):
@@ -130,6 +132,19 @@ def load(build_if_missing: bool = False):
                                         C.c_void_p, C.c_void_p]),
         "vf_batch_cluster_size": (C.c_int, [H, C.POINTER(VfBatchOptions), C.POINTER(C.c_int32)]),
         "vf_batch_last_error": (C.c_char_p, [C.c_void_p]),
+        "vf_server_create": (C.c_int, [C.c_int32, C.c_int64, C.POINTER(VfBatchOptions), C.c_int64,
+                                       C.POINTER(C.c_void_p)]),
+        "vf_server_submit": (C.c_int, [C.c_void_p, C.POINTER(VfConfig), C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p, C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.POINTER(C.c_int64)]),
+        "vf_server_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_int32)]),
+        "vf_server_result": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_int64),
+                                       C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
+        "vf_server_release": (C.c_int, [C.c_void_p, C.c_int64]),
+        "vf_server_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                      C.POINTER(C.c_int64)]),
+        "vf_server_destroy": (C.c_int, [C.c_void_p]),
+        "vf_server_last_error": (C.c_char_p, [C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -154,6 +169,18 @@ def check(lib, h, rc: int):
 def check_batch(lib, b, rc: int):
     if rc != VF_OK:
         msg = lib.vf_batch_last_error(b)
+        text = msg.decode() if msg else ""
+        if rc == VF_EINVAL:
+            from .api import ArgumentError
+            raise ArgumentError(text)
+        if rc == VF_ENOMEM:
+            raise MemoryError(text)
+        raise NativeError(rc, text)
+
+
+def check_server(lib, s, rc: int):
+    if rc != VF_OK:
+        msg = lib.vf_server_last_error(s)
         text = msg.decode() if msg else ""
         if rc == VF_EINVAL:
             from .api import ArgumentError

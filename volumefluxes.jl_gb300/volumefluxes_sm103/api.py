@@ -522,6 +522,80 @@ def _to_planes(new_state, nx: int, ny: int, dtype) -> list[np.ndarray]:
 
 
 # --------------------------------------------------------------------------- simulator
+def system_config(backend, system: "ConservedSystem", timestepper, grid: CartesianGrid, cfl: float) -> N.VfConfig:
+    """The C-ABI configuration of a ConservedSystem + Simulator (no device work)."""
+    s, g = system, grid
+    eq = s.equation
+    if not isinstance(eq, ShallowWaterEquations):
+        raise ArgumentError("the sm_103a backend runs ShallowWaterEquations (2D practical SWE) only")
+    if not isinstance(s.reconstruction, (LinearReconstruction, NoReconstruction)):
+        raise ArgumentError(f"{type(s.reconstruction).__name__} is not implemented on the sm_103a backend")
+    if not isinstance(s.numericalflux, CentralUpwind):
+        raise ArgumentError(f"{type(s.numericalflux).__name__} is not implemented on the sm_103a backend")
+    if not isinstance(g.boundary, (WallBC, PeriodicBC)):
+        raise ArgumentError(f"{type(g.boundary).__name__} is not implemented on the sm_103a backend "
+                            "(WallBC and PeriodicBC are)")
+    if g.gc != 2:
+        raise ArgumentError("the sm_103a backend needs CartesianGrid(...; gc=2)")
+    if isinstance(timestepper, RungeKutta2):
+        stepper = N.VF_STEPPER_RK2
+    elif isinstance(timestepper, ForwardEulerStepper):
+        stepper = N.VF_STEPPER_FE
+    else:
+        raise ArgumentError(f"{type(timestepper).__name__} is not implemented on the sm_103a backend")
+    cfg = N.VfConfig()
+    cfg.abi_version = N.VF_ABI_VERSION
+    cfg.nx, cfg.ny, cfg.gc = g.nx, g.ny, g.gc
+    for i, v in enumerate(g.extent.reshape(-1)):
+        cfg.extent[i] = float(v)
+    cfg.real_bytes = np.dtype(backend.realtype).itemsize
+    cfg.g, cfg.rho = eq.g, eq.rho
+    cfg.depth_cutoff, cfg.desingularizing_kappa = eq.depth_cutoff, eq.desingularizing_kappa
+    if isinstance(s.reconstruction, NoReconstruction):
+        cfg.reconstruction, cfg.theta = N.VF_REC_NONE, 0.0
+    else:
+        cfg.reconstruction, cfg.theta = N.VF_REC_LINEAR, s.reconstruction.theta
+    if len(s.source_terms) > N.VF_MAX_SOURCES:
+        raise ArgumentError("too many source terms")
+    for i, st in enumerate(s.source_terms):
+        if type(st) is SourceTermBottom:
+            cfg.source_kind[i], cfg.source_rate[i] = N.VF_SRC_BOTTOM, 0.0
+        elif isinstance(st, ConstantRain):
+            cfg.source_kind[i], cfg.source_rate[i] = N.VF_SRC_CONST_RAIN, st.rain_rate
+        elif isinstance(st, ConstantInfiltration):
+            cfg.source_kind[i], cfg.source_rate[i] = N.VF_SRC_CONST_INFIL, st.infiltration_rate
+        elif isinstance(st, TimeDependentRain):
+            cfg.source_kind[i] = N.VF_SRC_TIME_RAIN
+        elif isinstance(st, HortonInfiltration):
+            cfg.source_kind[i], cfg.source_rate[i] = N.VF_SRC_HORTON, st.fc
+            cfg.source_aux[i][0], cfg.source_aux[i][1] = st.f0, st.k
+        elif isinstance(st, FunctionalRain):
+            cfg.source_kind[i] = N.VF_SRC_RAIN_FIELD
+        else:
+            raise ArgumentError(f"{type(st).__name__} is not implemented on the sm_103a backend")
+    cfg.n_sources = len(s.source_terms)
+    fr = s.implicit_source_term
+    if fr is None:
+        cfg.friction, cfg.friction_Cz = N.VF_FRICTION_NONE, 0.0
+    elif isinstance(fr, ImplicitFriction):
+        if fr.friction_function not in _FRICTION_CODES:
+            raise ArgumentError("ImplicitFriction needs friction_bsa2012, friction_fcg2016 or friction_bh2021")
+        cfg.friction, cfg.friction_Cz = _FRICTION_CODES[fr.friction_function], fr.Cz
+    else:
+        raise ArgumentError(f"{type(fr).__name__} is not implemented on the sm_103a backend")
+    cfg.stepper = stepper
+    cfg.bc = N.VF_BC_PERIODIC if isinstance(g.boundary, PeriodicBC) else N.VF_BC_WALL
+    cfg.cfl = float(np.dtype(backend.realtype).type(cfl))
+    if isinstance(eq.B, ConstantBottomTopography):
+        cfg.bottom_is_constant, cfg.bottom_constant = 1, eq.B.B
+    elif isinstance(eq.B, BottomTopography2D):
+        cfg.bottom_is_constant, cfg.bottom_constant = 0, 0.0
+    else:
+        raise ArgumentError(f"{type(eq.B).__name__} is not supported")
+    cfg.device = backend.device
+    return cfg
+
+
 class Simulator:
     """Simulator(backend, system, timestepper, grid; cfl=0.25, t0=0.0), src/simulator.jl:60-91.
 
@@ -571,76 +645,7 @@ class Simulator:
             self._upload_field(i, st.field(self.t))
 
     def _config(self) -> N.VfConfig:
-        s, g = self.system, self.grid
-        eq = s.equation
-        if not isinstance(eq, ShallowWaterEquations):
-            raise ArgumentError("the sm_103a backend runs ShallowWaterEquations (2D practical SWE) only")
-        if not isinstance(s.reconstruction, (LinearReconstruction, NoReconstruction)):
-            raise ArgumentError(f"{type(s.reconstruction).__name__} is not implemented on the sm_103a backend")
-        if not isinstance(s.numericalflux, CentralUpwind):
-            raise ArgumentError(f"{type(s.numericalflux).__name__} is not implemented on the sm_103a backend")
-        if not isinstance(g.boundary, (WallBC, PeriodicBC)):
-            raise ArgumentError(f"{type(g.boundary).__name__} is not implemented on the sm_103a backend "
-                                "(WallBC and PeriodicBC are)")
-        if g.gc != 2:
-            raise ArgumentError("the sm_103a backend needs CartesianGrid(...; gc=2)")
-        if isinstance(self.timestepper, RungeKutta2):
-            stepper = N.VF_STEPPER_RK2
-        elif isinstance(self.timestepper, ForwardEulerStepper):
-            stepper = N.VF_STEPPER_FE
-        else:
-            raise ArgumentError(f"{type(self.timestepper).__name__} is not implemented on the sm_103a backend")
-        cfg = N.VfConfig()
-        cfg.abi_version = N.VF_ABI_VERSION
-        cfg.nx, cfg.ny, cfg.gc = g.nx, g.ny, g.gc
-        for i, v in enumerate(g.extent.reshape(-1)):
-            cfg.extent[i] = float(v)
-        cfg.real_bytes = self.dtype.itemsize
-        cfg.g, cfg.rho = eq.g, eq.rho
-        cfg.depth_cutoff, cfg.desingularizing_kappa = eq.depth_cutoff, eq.desingularizing_kappa
-        if isinstance(s.reconstruction, NoReconstruction):
-            cfg.reconstruction, cfg.theta = N.VF_REC_NONE, 0.0
-        else:
-            cfg.reconstruction, cfg.theta = N.VF_REC_LINEAR, s.reconstruction.theta
-        if len(s.source_terms) > N.VF_MAX_SOURCES:
-            raise ArgumentError("too many source terms")
-        for i, st in enumerate(s.source_terms):
-            if type(st) is SourceTermBottom:
-                cfg.source_kind[i], cfg.source_rate[i] = N.VF_SRC_BOTTOM, 0.0
-            elif isinstance(st, ConstantRain):
-                cfg.source_kind[i], cfg.source_rate[i] = N.VF_SRC_CONST_RAIN, st.rain_rate
-            elif isinstance(st, ConstantInfiltration):
-                cfg.source_kind[i], cfg.source_rate[i] = N.VF_SRC_CONST_INFIL, st.infiltration_rate
-            elif isinstance(st, TimeDependentRain):
-                cfg.source_kind[i] = N.VF_SRC_TIME_RAIN
-            elif isinstance(st, HortonInfiltration):
-                cfg.source_kind[i], cfg.source_rate[i] = N.VF_SRC_HORTON, st.fc
-                cfg.source_aux[i][0], cfg.source_aux[i][1] = st.f0, st.k
-            elif isinstance(st, FunctionalRain):
-                cfg.source_kind[i] = N.VF_SRC_RAIN_FIELD
-            else:
-                raise ArgumentError(f"{type(st).__name__} is not implemented on the sm_103a backend")
-        cfg.n_sources = len(s.source_terms)
-        fr = s.implicit_source_term
-        if fr is None:
-            cfg.friction, cfg.friction_Cz = N.VF_FRICTION_NONE, 0.0
-        elif isinstance(fr, ImplicitFriction):
-            if fr.friction_function not in _FRICTION_CODES:
-                raise ArgumentError("ImplicitFriction needs friction_bsa2012, friction_fcg2016 or friction_bh2021")
-            cfg.friction, cfg.friction_Cz = _FRICTION_CODES[fr.friction_function], fr.Cz
-        else:
-            raise ArgumentError(f"{type(fr).__name__} is not implemented on the sm_103a backend")
-        cfg.stepper = stepper
-        cfg.bc = N.VF_BC_PERIODIC if isinstance(g.boundary, PeriodicBC) else N.VF_BC_WALL
-        cfg.cfl = self.cfl
-        if isinstance(eq.B, ConstantBottomTopography):
-            cfg.bottom_is_constant, cfg.bottom_constant = 1, eq.B.B
-        elif isinstance(eq.B, BottomTopography2D):
-            cfg.bottom_is_constant, cfg.bottom_constant = 0, 0.0
-        else:
-            raise ArgumentError(f"{type(eq.B).__name__} is not supported")
-        cfg.device = self.backend.device
-        return cfg
+        return system_config(self.backend, self.system, self.timestepper, self.grid, self.cfl)
 
     # -- lifecycle
     def close(self):

@@ -27,12 +27,14 @@ class BatchOptions:
     """Work granularity of the batch: a simulation with k 32x16 tiles gets the
     smallest power-of-two cluster c <= max_cluster with c * tiles_per_cta >= k;
     Float32 column-marching members split their strips into segments of
-    seg_rows rows. None keeps the library default. time_limit_s bounds the
-    batch's device time from its start (watchdog)."""
+    seg_rows rows; members of at least wide_cells cells run the whole-grid
+    kernels instead of a cluster. None keeps the library default. time_limit_s
+    bounds the batch's device time from its start (watchdog)."""
     tiles_per_cta: int | None = None
     max_cluster: int | None = None
     time_limit_s: float | None = None
     seg_rows: int | None = None
+    wide_cells: int | None = None  # members this large run the whole-grid kernels; -1: never
 
     def native(self) -> N.VfBatchOptions:
         o = N.VfBatchOptions()
@@ -40,6 +42,7 @@ class BatchOptions:
         o.max_cluster = int(self.max_cluster or 0)
         o.time_limit_s = float(self.time_limit_s or 0.0)
         o.seg_rows = int(self.seg_rows or 0)
+        o.wide_cells = int(self.wide_cells or 0)
         return o
 
 

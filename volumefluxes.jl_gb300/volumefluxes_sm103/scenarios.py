@@ -94,8 +94,8 @@ class Scenario:
             st.append(vf.ConstantInfiltration(self.infiltration_m_per_s))
         return st
 
-    def build(self, backend: vf.SM103Backend) -> vf.Simulator:
-        """The scenario script, written against the reference's API."""
+    def system(self, backend: vf.SM103Backend):
+        """(ConservedSystem, time stepper, grid) of the scenario script."""
         grid = self.grid()
         bottom = vf.ConstantBottomTopography() if self.B is None else vf.BottomTopography2D(self.B, backend, grid)
         eq = vf.ShallowWaterEquations(bottom, **self.eq)
@@ -107,6 +107,16 @@ class Scenario:
         rec = vf.NoReconstruction() if self.reconstruction == "none" else vf.LinearReconstruction(self.theta)
         system = vf.ConservedSystem(backend, rec, vf.CentralUpwind(eq), eq, grid, self.source_terms(), friction)
         stepper = vf.RungeKutta2() if self.stepper == "rk2" else vf.ForwardEulerStepper()
+        return system, stepper, grid
+
+    def config(self, backend: vf.SM103Backend):
+        """The C-ABI configuration of the scenario (no device work)."""
+        system, stepper, grid = self.system(backend)
+        return vf.system_config(backend, system, stepper, grid, self.cfl)
+
+    def build(self, backend: vf.SM103Backend) -> vf.Simulator:
+        """The scenario script, written against the reference's API."""
+        system, stepper, grid = self.system(backend)
         sim = vf.Simulator(backend, system, stepper, grid, cfl=self.cfl, t0=self.t0)
         vf.set_current_state(sim, (self.w0, self.hu0, self.hv0))
         return sim
@@ -198,3 +208,23 @@ def ensemble_member(spec: EnsembleSpec) -> Scenario:
                     cfl=0.25, rain_m_per_h=spec.rain_m_per_s * 3600, manning_n=spec.manning_n, bottom_source=True,
                     eq={"depth_cutoff": ENSEMBLE_DEPTH_CUTOFF},
                     meta={"seed": spec.seed, "n_hills": spec.n_hills, "endtime": spec.endtime, "h0": spec.h0})
+
+
+@dataclass
+class ServingSpec:
+    spec: EnsembleSpec
+    real: str  # "f32" or "f64"
+
+
+def serving_specs(count: int = 48, seed: int = 20241204, side_range=(128, 2048),
+                  endtime_range=(2.0, 20.0)) -> list[ServingSpec]:
+    """Requests of the serving workload: ensemble members with sides
+    log-uniform in side_range, Float32 or Float64 with probability 1/2 each, end
+    times uniform in endtime_range (rounded to Float32 values)."""
+    rng = SplitMix64(seed ^ 0x5EC0)
+    base = ensemble_specs(count, seed=seed, side_range=side_range)
+    out = []
+    for sp in base:
+        sp.endtime = float(np.float32(rng.uniform(*endtime_range)))
+        out.append(ServingSpec(sp, "f32" if rng.uniform() < 0.5 else "f64"))
+    return out
