@@ -240,25 +240,30 @@ const char* vf_batch_last_error(vf_batch* b);
  * A request is a configuration, its bottom corners, an initial interior state,
  * t0 and an end time; the engine keeps its state on the device from admission
  * to completion and writes the final interior state to the caller's output
- * buffers. Admission is oldest-first and bounded by an HBM budget (the device
- * bytes vf_create allocates per request); every poll launches what it
- * admitted as one batch beside the batches still running (continuous
- * batching). Requests take SourceTermBottom, ConstantRain and
- * ConstantInfiltration sources. Input buffers must stay valid until the
- * request is admitted, output buffers until it is reported done. */
+ * buffers. An engine thread per server admits requests oldest-first within an
+ * HBM budget (the device bytes vf_create allocates per request), launches
+ * each round's admissions as one batch beside the batches still running
+ * (continuous batching) and completes requests as their done flags appear.
+ * Requests take SourceTermBottom, ConstantRain and ConstantInfiltration
+ * sources. Input buffers must stay valid until the request is admitted,
+ * output buffers until it is reported done. */
 typedef struct vf_server vf_server;
 
-/* opt: batch options of every launch (NULL: defaults); max_steps <= 0: none. */
+/* opt: batch options of every launch (NULL: defaults, except wide_cells, which
+ * defaults to 262144 here: requests arrive a few at a time); max_steps <= 0: none. */
 int vf_server_create(int32_t device, int64_t hbm_budget_bytes, const vf_batch_options* opt, int64_t max_steps,
                      vf_server** out);
 /* Queues a request; *ticket_out identifies it. VF_ENOMEM if it alone exceeds the budget. */
 int vf_server_submit(vf_server* s, const vf_config* cfg, const void* B_corners, const void* w, const void* hu,
                      const void* hv, double t0, double endtime, void* out_w, void* out_hu, void* out_hv,
                      int64_t* ticket_out);
-/* Advances the engine (complete, admit, launch) without waiting on the GPU.
- * Writes up to `capacity` tickets that finished during this call (done or
- * failed) to done_tickets and their count to *n_done. */
+/* Non-blocking: writes up to `capacity` tickets that finished (done or failed)
+ * since the last poll to done_tickets and their count to *n_done. Returns
+ * VF_ECUDA once if the engine met a launch error since the last poll. */
 int vf_server_poll(vf_server* s, int64_t* done_tickets, int32_t capacity, int32_t* n_done);
+/* When the request was submitted, admitted and finished, in seconds since the
+ * server was created. */
+int vf_server_timing(vf_server* s, int64_t ticket, double* submit_s, double* admit_s, double* done_s);
 /* Outcome of a finished request: final time, steps, last dt, VF_BATCH_*
  * status; returns the request's error code if it failed. */
 int vf_server_result(vf_server* s, int64_t ticket, double* t_out, int64_t* steps_out, double* last_dt_out,

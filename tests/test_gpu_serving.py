@@ -26,6 +26,13 @@ def requests(n, seed=5, side_cap=200):
     return out
 
 
+def wait_for(srv, cond, timeout=60.0):
+    t0 = time.time()
+    while not cond(srv.stats()):
+        assert time.time() - t0 < timeout, srv.stats()
+        time.sleep(0.0005)
+
+
 def drain(srv, tickets, timeout=300.0):
     done = {}
     t0 = time.time()
@@ -67,7 +74,7 @@ def test_request_is_the_same_alone_and_in_the_mix(real):
     others = requests(5, seed=9)
     with Server(8 * GB) as srv:
         first = [srv.submit(sc, r, t) for sc, r, t in others[:3]]
-        srv.poll()  # the first three start
+        wait_for(srv, lambda st: st["running"] == 3)  # the first three run
         mid = srv.submit(probe, real, T)  # arrives while they run
         last = [srv.submit(sc, r, t) for sc, r, t in others[3:]]
         res = drain(srv, first + [mid] + last)
@@ -82,17 +89,18 @@ def test_admission_waits_for_memory():
     sc = hills_rect(128, 128)
     need = 0
     with Server(1 << 40) as srv:  # measure one request's charge
-        tk = srv.submit(sc, np.float64, 1.0)
-        srv.poll()
+        tk = srv.submit(sc, np.float64, 30.0)
+        wait_for(srv, lambda st: st["running"] == 1)
         need = srv.stats()["used_bytes"]
         drain(srv, [tk])
     assert need > 0
     with Server(2 * need + need // 2) as srv:  # room for two at a time
-        tickets = [srv.submit(sc, np.float64, 3.0) for _ in range(5)]
-        srv.poll()
+        tickets = [srv.submit(sc, np.float64, 30.0) for _ in range(5)]
+        wait_for(srv, lambda st: st["running"] == 2)
         st = srv.stats()
-        assert st["running"] == 2 and st["queued"] == 3 and st["used_bytes"] == 2 * need
+        assert st["queued"] == 3 and st["used_bytes"] == 2 * need
         res = drain(srv, tickets)
+        assert max(r.admit_s for r in res[2:]) >= min(r.done_s for r in res[:2])  # admitted as memory freed
         assert srv.stats()["used_bytes"] == 0
-    assert all(r.status == N.VF_BATCH_OK and r.t == 3.0 for r in res)
+    assert all(r.status == N.VF_BATCH_OK and r.t == 30.0 for r in res)
     assert all(np.array_equal(r.state.h, res[0].state.h) for r in res)

@@ -14,8 +14,8 @@
 // Simulations of at least wide_cells interior cells are "wide": a 16-CTA
 // cluster would leave most of the GPU to them alone, so they run the plain
 // whole-grid step kernels on their handle's stream instead, as the device loop
-// of vf_simulate, in chunks of kChunk steps captured once as a CUDA graph. Two
-// chunks are kept in flight; after each, the step record is copied to pinned
+// of vf_simulate, in chunks of kChunk steps captured once as a CUDA graph.
+// kInFlight chunks are kept queued; after each, the step record is copied to pinned
 // memory behind an event, and the host retires chunks and enqueues new ones
 // whenever the batch is polled. Their kernels share the SMs with the cluster
 // launches, and their results are those of vf_simulate.
@@ -44,9 +44,9 @@ struct Wide {
   int member = 0;
   long long enqueued = 0;      // steps enqueued so far
   long long max_steps = 0;
-  int head = 0, inflight = 0;  // chunks head .. head+inflight-1 are in flight; chunk c uses ev/rec slot c & 1
-  long long chunk_end[2] = {0, 0};
-  cudaEvent_t ev[2] = {nullptr, nullptr};
+  int head = 0, inflight = 0;  // chunks head .. head+inflight-1 are in flight; chunk c uses ev/rec slot c % 3
+  long long chunk_end[3] = {0, 0, 0};
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   double last_t = 0;
   bool done = false;
 };
@@ -84,7 +84,7 @@ int bfail(vf_batch* b, int code, const std::string& msg) {
 // two step-record copies of the chunks in flight.
 struct Slot {
   vf::EnsResult res;
-  vf::StepRecord rec[2];
+  vf::StepRecord rec[3];
 };
 
 constexpr int kSlab = 4096;
@@ -247,7 +247,8 @@ void destroy_batch(vf_batch* b) {
   delete b;
 }
 
-constexpr int kChunk = 16;  // steps per graph launch of a wide member
+constexpr int kChunk = 16;    // steps per graph launch of a wide member
+constexpr int kInFlight = 3;  // chunks kept queued per wide member (rides out host stalls)
 
 // Final result of a wide member from the record copy of its last retired chunk.
 void wide_finish(vf_batch* b, Wide& w, const vf::StepRecord& r, long long k, int status) {
@@ -270,7 +271,7 @@ int wide_enqueue(vf_batch* b, Wide& w) {
                                                   : vf::handle_enqueue_steps(h, w.enqueued, n);
   if (rc) return rc;
   w.enqueued += n;
-  const int slot = (w.head + w.inflight) & 1;
+  const int slot = (w.head + w.inflight) % kInFlight;
   cudaError_t e = cudaMemcpyAsync(slot_rec(b->slots[w.member], slot), h->rec, sizeof(vf::StepRecord),
                                   cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaEventRecord(w.ev[slot], h->stream);
@@ -289,7 +290,7 @@ int pump(vf_batch* b) {
   for (Wide& w : b->wide) {
     if (w.done) continue;
     while (w.inflight > 0) {
-      const int slot = w.head & 1;
+      const int slot = w.head % kInFlight;
       const cudaError_t q = cudaEventQuery(w.ev[slot]);
       if (q == cudaErrorNotReady) break;
       if (q != cudaSuccess) return bfail(b, VF_ECUDA, std::string("wide member: ") + cudaGetErrorString(q));
@@ -316,11 +317,11 @@ int pump(vf_batch* b) {
       }
     }
     if (!w.done && late && w.inflight == 0) {
-      const int last = (w.head - 1) & 1;
+      const int last = (w.head + kInFlight - 1) % kInFlight;
       wide_finish(b, w, *slot_rec(b->slots[w.member], last), w.chunk_end[last], vf::kEnsTimeout);
     }
     if (w.done || late) continue;
-    while (w.inflight < 2 && w.enqueued < w.max_steps)
+    while (w.inflight < kInFlight && w.enqueued < w.max_steps)
       if (int rc = wide_enqueue(b, w)) return bfail(b, rc, "wide member launch: " + b->hs[w.member]->err);
   }
   return VF_OK;
@@ -402,11 +403,11 @@ int vf_batch_launch(vf_handle* const* hs, int32_t n, const double* t0, const dou
   // Wide members start first: their first two chunks go in before any cluster.
   for (Wide& w : b->wide) {
     vf_handle* h = hs[w.member];
-    bool ok = cudaEventCreateWithFlags(&w.ev[0], cudaEventDisableTiming) == cudaSuccess &&
-              cudaEventCreateWithFlags(&w.ev[1], cudaEventDisableTiming) == cudaSuccess;
+    bool ok = true;
+    for (cudaEvent_t& e : w.ev) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
     int rc = ok ? vf::handle_begin_loop(h, t0[w.member], endtime[w.member], match_endtime, maximum_timestep)
                 : VF_ECUDA;
-    for (int k = 0; rc == VF_OK && k < 2 && w.enqueued < w.max_steps; ++k) rc = wide_enqueue(b, w);
+    for (int k = 0; rc == VF_OK && k < kInFlight && w.enqueued < w.max_steps; ++k) rc = wide_enqueue(b, w);
     if (rc) {
       cudaGetLastError();
       for (Wide& x : b->wide) cudaStreamSynchronize(hs[x.member]->stream);
@@ -552,7 +553,7 @@ int vf_batch_wait(vf_batch* b) {
     if (all) break;
     for (Wide& w : b->wide)
       if (!w.done && w.inflight > 0) {
-        cudaEventSynchronize(w.ev[w.head & 1]);
+        cudaEventSynchronize(w.ev[w.head % kInFlight]);
         break;
       }
   }

@@ -2,7 +2,7 @@
 //
 // Requests are whole flood simulations: a configuration, a bottom, an initial
 // interior state and an end time, with output buffers for the final state.
-// The engine is driven by the caller's vf_server_poll() and does, each time:
+// An engine thread runs, in a loop:
 //   1. completion: every running request whose done flag is set (the batch's
 //      pinned, mapped result slot) is collected, its final interior state is
 //      copied to the caller's buffers, its handle is destroyed and its device
@@ -10,20 +10,27 @@
 //   2. admission: queued requests, oldest first, get a handle (device memory
 //      from the library pool), their bottom and state are uploaded, and their
 //      bytes are charged, for as long as the HBM budget holds;
-//   3. launch: everything admitted in this poll starts as one batch
+//   3. launch: everything admitted in this round starts as one batch
 //      (vf_batch_launch) on its own streams, while earlier batches keep
 //      running: continuous batching, with the GPU's block scheduler sharing the
 //      SMs between the batches in flight.
 // A request's result does not depend on what runs beside it: each simulation
-// is one cluster with its own dt and its own data.
+// is one cluster (or one whole-grid kernel stream) with its own dt and data.
+//
+// The loop also feeds the wide members of running batches, about every 100 us
+// while anything runs (it sleeps otherwise), so the GPU never waits for the
+// caller; the caller's submit/poll/result calls only take the engine's lock.
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <condition_variable>
 #include <cstring>
 #include <deque>
 #include <map>
+#include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "vf_handle.h"
@@ -52,6 +59,8 @@ struct Request {
   int32_t status = 0;
   int error = 0;
   std::string message;
+  bool reported = false;
+  double submit_s = 0, admit_s = 0, done_s = 0;  // seconds since the server started
 };
 
 struct Batch {
@@ -72,7 +81,13 @@ struct vf_server {
   std::map<int64_t, Request> reqs;
   std::vector<Batch> batches;
   int64_t launches = 0;
-  std::string err;
+  std::string err;        // last caller-side error
+  std::string engine_err; // last engine error (reported by the next poll)
+  std::chrono::steady_clock::time_point t0;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::thread engine;
+  bool stop = false;
 };
 
 namespace {
@@ -85,7 +100,12 @@ int sfail(vf_server* s, int code, const std::string& msg) {
   return code;
 }
 
+double now_s(const vf_server* s) {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - s->t0).count();
+}
+
 void finish_request(vf_server* s, Request& r, int error, const std::string& msg) {
+  r.done_s = now_s(s);
   if (r.h) {
     vf_destroy(r.h);
     r.h = nullptr;
@@ -151,6 +171,7 @@ int admit_and_launch(vf_server* s) {
     Request& r = s->reqs[tk];
     if (s->used + r.bytes > s->budget) break;  // oldest first: wait for memory
     s->queue.pop_front();
+    r.admit_s = now_s(s);
     if (!admit(s, r)) continue;
     hs.push_back(r.h);
     t0.push_back(r.t0);
@@ -164,7 +185,8 @@ int admit_and_launch(vf_server* s) {
   if (rc) {
     const std::string msg = vf_batch_last_error(nullptr);
     for (int64_t tk : tickets) finish_request(s, s->reqs[tk], rc, msg);
-    return sfail(s, rc, "batch launch: " + msg);
+    s->engine_err = "batch launch: " + msg;
+    return rc;
   }
   s->batches.push_back(Batch{b, (int)hs.size()});
   s->launches += 1;
@@ -176,6 +198,33 @@ int admit_and_launch(vf_server* s) {
     r.slot = (int)i;
   }
   return VF_OK;
+}
+
+bool busy(const vf_server* s) {
+  if (!s->queue.empty()) return true;
+  for (const auto& kv : s->reqs)
+    if (kv.second.state == ReqState::kRunning) return true;
+  return false;
+}
+
+// The engine thread: complete, admit, launch, feed wide members; about every
+// 100 us while anything runs, asleep otherwise.
+void engine_loop(vf_server* s) {
+  cudaSetDevice(s->device);
+  std::unique_lock<std::mutex> lk(s->mu);
+  while (!s->stop) {
+    complete(s);
+    admit_and_launch(s);
+    for (Batch& bt : s->batches) {
+      int32_t nd = 0;
+      if (bt.b) vf_batch_poll(bt.b, &nd);  // retires and refills wide members' chunks
+    }
+    if (busy(s)) {
+      s->cv.wait_for(lk, std::chrono::microseconds(100));
+    } else {
+      s->cv.wait(lk, [s] { return s->stop || !s->queue.empty(); });
+    }
+  }
 }
 
 }  // namespace
@@ -192,9 +241,20 @@ int vf_server_create(int32_t device, int64_t hbm_budget_bytes, const vf_batch_op
   s->device = device;
   s->budget = (size_t)hbm_budget_bytes;
   s->max_steps = max_steps;
+  // Requests usually arrive a few at a time, so a cluster would leave most of
+  // the GPU idle: members from 512^2 cells up take the whole-grid kernels.
+  s->opt.wide_cells = 1LL << 18;
+  s->has_opt = true;
   if (opt) {
     s->opt = *opt;
-    s->has_opt = true;
+    if (opt->wide_cells == 0) s->opt.wide_cells = 1LL << 18;
+  }
+  s->t0 = std::chrono::steady_clock::now();
+  try {
+    s->engine = std::thread(engine_loop, s);
+  } catch (...) {
+    delete s;
+    return sfail(nullptr, VF_ENOMEM, "engine thread could not start");
   }
   *out = s;
   return VF_OK;
@@ -223,36 +283,43 @@ int vf_server_submit(vf_server* s, const vf_config* cfg, const void* B_corners, 
   r.endtime = endtime;
   r.bytes = vf::handle_device_bytes(cfg);
   if (r.bytes > s->budget) return sfail(s, VF_ENOMEM, "request larger than the whole HBM budget");
-  const int64_t tk = s->next_ticket++;
-  s->reqs.emplace(tk, r);
-  s->queue.push_back(tk);
-  *ticket_out = tk;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    r.submit_s = now_s(s);
+    const int64_t tk = s->next_ticket++;
+    s->reqs.emplace(tk, r);
+    s->queue.push_back(tk);
+    *ticket_out = tk;
+  }
+  s->cv.notify_one();
   return VF_OK;
 }
 
 int vf_server_poll(vf_server* s, int64_t* done_tickets, int32_t capacity, int32_t* n_done) {
   if (!s) return sfail(s, VF_EINVAL, "NULL server");
-  if (cudaSetDevice(s->device) != cudaSuccess) return sfail(s, VF_ECUDA, "cudaSetDevice failed");
-  std::vector<int64_t> before;
-  for (auto& kv : s->reqs)
-    if (kv.second.state == ReqState::kRunning || kv.second.state == ReqState::kQueued) before.push_back(kv.first);
-  complete(s);
-  int rc = admit_and_launch(s);
+  std::lock_guard<std::mutex> lk(s->mu);
   int32_t n = 0;
-  for (int64_t tk : before) {
-    const Request& r = s->reqs[tk];
-    if (r.state == ReqState::kDone || r.state == ReqState::kFailed) {
-      if (done_tickets && n < capacity) done_tickets[n] = tk;
+  for (auto& kv : s->reqs) {
+    Request& r = kv.second;
+    if ((r.state == ReqState::kDone || r.state == ReqState::kFailed) && !r.reported && n < capacity) {
+      if (done_tickets) done_tickets[n] = kv.first;
+      r.reported = true;
       ++n;
     }
   }
   if (n_done) *n_done = n;
-  return rc;
+  if (!s->engine_err.empty()) {
+    s->err = s->engine_err;
+    s->engine_err.clear();
+    return VF_ECUDA;
+  }
+  return VF_OK;
 }
 
 int vf_server_result(vf_server* s, int64_t ticket, double* t_out, int64_t* steps_out, double* last_dt_out,
                      int32_t* status_out) {
   if (!s) return sfail(s, VF_EINVAL, "NULL server");
+  std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->reqs.find(ticket);
   if (it == s->reqs.end()) return sfail(s, VF_EINVAL, "unknown ticket");
   const Request& r = it->second;
@@ -265,8 +332,20 @@ int vf_server_result(vf_server* s, int64_t ticket, double* t_out, int64_t* steps
   return VF_OK;
 }
 
+int vf_server_timing(vf_server* s, int64_t ticket, double* submit_s, double* admit_s, double* done_s) {
+  if (!s) return sfail(s, VF_EINVAL, "NULL server");
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return sfail(s, VF_EINVAL, "unknown ticket");
+  if (submit_s) *submit_s = it->second.submit_s;
+  if (admit_s) *admit_s = it->second.admit_s;
+  if (done_s) *done_s = it->second.done_s;
+  return VF_OK;
+}
+
 int vf_server_release(vf_server* s, int64_t ticket) {
   if (!s) return sfail(s, VF_EINVAL, "NULL server");
+  std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->reqs.find(ticket);
   if (it == s->reqs.end()) return sfail(s, VF_EINVAL, "unknown ticket");
   if (it->second.state == ReqState::kQueued || it->second.state == ReqState::kRunning)
@@ -277,6 +356,7 @@ int vf_server_release(vf_server* s, int64_t ticket) {
 
 int vf_server_stats(vf_server* s, int64_t* used_bytes, int32_t* queued, int32_t* running, int64_t* launches) {
   if (!s) return sfail(s, VF_EINVAL, "NULL server");
+  std::lock_guard<std::mutex> lk(s->mu);
   int32_t q = 0, r = 0;
   for (auto& kv : s->reqs) {
     q += kv.second.state == ReqState::kQueued;
@@ -291,6 +371,12 @@ int vf_server_stats(vf_server* s, int64_t* used_bytes, int32_t* queued, int32_t*
 
 int vf_server_destroy(vf_server* s) {
   if (!s) return VF_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv.notify_one();
+  if (s->engine.joinable()) s->engine.join();
   cudaSetDevice(s->device);
   for (Batch& bt : s->batches)
     if (bt.b) vf_batch_free(bt.b);

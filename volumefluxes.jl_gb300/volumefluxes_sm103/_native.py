@@ -32,7 +32,8 @@ EXPORTED_SYMBOLS = (
     "vf_water_volume_static",
     "vf_batch_launch", "vf_batch_poll", "vf_batch_is_done", "vf_batch_collect", "vf_batch_wait", "vf_batch_free",
     "vf_batch_simulate", "vf_batch_cluster_size", "vf_batch_last_error",
-    "vf_server_create", "vf_server_submit", "vf_server_poll", "vf_server_result", "vf_server_release",
+    "vf_server_create", "vf_server_submit", "vf_server_poll", "vf_server_result", "vf_server_timing",
+    "vf_server_release",
     "vf_server_stats", "vf_server_destroy", "vf_server_last_error",
 )
 VF_BATCH_OK, VF_BATCH_TIMEOUT, VF_BATCH_STALLED, VF_BATCH_MAX_STEPS = 0, 1, 2, 3
@@ -140,6 +141,8 @@ def load(build_if_missing: bool = False):
         "vf_server_poll": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_int32)]),
         "vf_server_result": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_int64),
                                        C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
+        "vf_server_timing": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]),
         "vf_server_release": (C.c_int, [C.c_void_p, C.c_int64]),
         "vf_server_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                       C.POINTER(C.c_int64)]),

@@ -27,6 +27,29 @@ class ServeResult:
     last_dt: float
     status: int
     state: StateView  # final interior (h, hu, hv), each (nx, ny)
+    submit_s: float = 0.0  # engine clock: seconds since the server was created
+    admit_s: float = 0.0
+    done_s: float = 0.0
+
+    @property
+    def latency_s(self) -> float:
+        return self.done_s - self.submit_s
+
+
+class Request:
+    """A request's configuration and arrays in the library's layout, prepared
+    ahead of submission so that submitting costs no host copies."""
+
+    def __init__(self, scenario, realtype, endtime: float, device: int = 0):
+        be = SM103Backend(realtype, device=device)
+        self.cfg = scenario.config(be)
+        dt = np.dtype(realtype)
+        self.B = None if scenario.B is None else np.ascontiguousarray(np.asarray(scenario.B, dtype=dt).T)
+        self.w, self.hu, self.hv = (np.ascontiguousarray(np.asarray(a, dtype=dt).T)
+                                    for a in (scenario.w0, scenario.hu0, scenario.hv0))
+        self.out = [np.empty((scenario.ny, scenario.nx), dtype=dt) for _ in range(3)]
+        self.t0 = float(scenario.t0)
+        self.endtime = float(endtime)
 
 
 class Server:
@@ -41,23 +64,19 @@ class Server:
         self.device = device
         self._live = {}  # ticket -> arrays the engine reads or writes
 
-    def submit(self, scenario, realtype, endtime: float) -> int:
-        """Queue one request; returns its ticket. The scenario's arrays are copied now."""
-        be = SM103Backend(realtype, device=self.device)
-        cfg = scenario.config(be)
-        dt = np.dtype(realtype)
-        B = None if scenario.B is None else np.ascontiguousarray(np.asarray(scenario.B, dtype=dt).T)
-        w, hu, hv = (np.ascontiguousarray(np.asarray(a, dtype=dt).T) for a in (scenario.w0, scenario.hu0, scenario.hv0))
-        out = [np.empty((scenario.ny, scenario.nx), dtype=dt) for _ in range(3)]
+    def submit(self, scenario, realtype=None, endtime: float | None = None) -> int:
+        """Queue one request (a Request, or a scenario with its real type and end
+        time); returns its ticket."""
+        req = scenario if isinstance(scenario, Request) else Request(scenario, realtype, endtime, self.device)
         tk = C.c_int64()
         N.check_server(self._lib, self._s, self._lib.vf_server_submit(
-            self._s, C.byref(cfg), None if B is None else N.ptr(B), N.ptr(w), N.ptr(hu), N.ptr(hv),
-            float(scenario.t0), float(endtime), N.ptr(out[0]), N.ptr(out[1]), N.ptr(out[2]), C.byref(tk)))
-        self._live[tk.value] = (B, w, hu, hv, out)
+            self._s, C.byref(req.cfg), None if req.B is None else N.ptr(req.B), N.ptr(req.w), N.ptr(req.hu),
+            N.ptr(req.hv), req.t0, req.endtime, N.ptr(req.out[0]), N.ptr(req.out[1]), N.ptr(req.out[2]), C.byref(tk)))
+        self._live[tk.value] = req
         return tk.value
 
     def poll(self, capacity: int = 4096) -> list[int]:
-        """Advance the engine; tickets that finished during this call."""
+        """Tickets that finished since the last poll (non-blocking)."""
         buf = (C.c_int64 * capacity)()
         n = C.c_int32()
         N.check_server(self._lib, self._s, self._lib.vf_server_poll(self._s, buf, capacity, C.byref(n)))
@@ -67,8 +86,12 @@ class Server:
         t, st, ldt, s = C.c_double(), C.c_int64(), C.c_double(), C.c_int32()
         N.check_server(self._lib, self._s, self._lib.vf_server_result(self._s, int(ticket), C.byref(t), C.byref(st),
                                                                       C.byref(ldt), C.byref(s)))
-        out = self._live[ticket][4]
-        res = ServeResult(t.value, st.value, ldt.value, s.value, StateView(*(o.T for o in out)))
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        N.check_server(self._lib, self._s, self._lib.vf_server_timing(self._s, int(ticket), C.byref(a), C.byref(b),
+                                                                      C.byref(c)))
+        out = self._live[ticket].out
+        res = ServeResult(t.value, st.value, ldt.value, s.value, StateView(*(o.T for o in out)), a.value, b.value,
+                          c.value)
         if release:
             N.check_server(self._lib, self._s, self._lib.vf_server_release(self._s, int(ticket)))
             del self._live[ticket]
