@@ -69,6 +69,11 @@ def parse():
     ap.add_argument("--serving-requests", type=int, default=48)
     ap.add_argument("--serving-rates", default="10,100,1000", help="Poisson arrival rates [req/s]")
     ap.add_argument("--serving-budget-gb", type=float, default=120.0)
+    ap.add_argument("--adjoint", action="store_true", help="also measure the differentiation workload (~1-2 min)")
+    ap.add_argument("--adjoint-n", type=int, default=512)
+    ap.add_argument("--adjoint-steps", type=int, default=400)
+    ap.add_argument("--adjoint-fd-dirs", type=int, default=64)
+    ap.add_argument("--adjoint-dual-dirs", type=int, default=2)
     return ap.parse_args()
 
 
@@ -538,6 +543,104 @@ def measure_serving(args, local):
     return out
 
 
+def adjoint_workload(n, steps):
+    return (f"differentiation: {n}x{n} cells (Δ = 1 m), 16 seeded hills (amplitude U[0.2,1] m, width U[50,200] m) + "
+            f"1e-3 slope, depth 1 m, Manning n = 0.03, rain 2e-5 m/s, wall BCs, RK2, CFL 0.25, {steps} steps with the "
+            "dt sequence frozen from the forward pass; loss = sum over 32 seeded gauges of (w - w_target)^2, "
+            "w_target from the same steps on a perturbed terrain; gradient w.r.t. every bottom corner "
+            f"({(n + 5) ** 2} values) and Manning n")
+
+
+def measure_adjoint(args, local):
+    """Gradient of the gauge loss by the GPU reverse sweep, checked against
+    central differences (smooth random directions) and the oracle on dual numbers."""
+    import volumefluxes_sm103 as vf
+    from volumefluxes_sm103 import adjoint as AD
+    from volumefluxes_sm103 import scenarios as S
+    from oracle import vf_oracle as O
+    case = S.differentiation_case(args.adjoint_n)
+    sc, gauges, steps = case.scenario, case.gauges, args.adjoint_steps
+    out = {"workload": adjoint_workload(args.adjoint_n, steps), "checkpoint_every": int(round(math.sqrt(steps)))}
+    grads = {}
+    dts = None
+    for real in (np.float64, np.float32):
+        name = "f64" if real == np.float64 else "f32"
+        sim = sc.build(vf.SM103Backend(real, device=local))
+        adj = AD.GaugeAdjoint(sim, steps)
+        t0 = time.perf_counter()
+        d = adj.forward(dts)
+        t1 = time.perf_counter()
+        if dts is None:
+            dts = d
+            target = AD.gauge_values(sc, np.float64, gauges, dts, B=case.B_target)
+        t2 = time.perf_counter()
+        loss, gB, gCz = adj.backward(gauges, target)
+        t3 = time.perf_counter()
+        adj.close()
+        sim.close()
+        gn = gCz * 2 * sc.manning_n
+        grads[name] = (loss, gB, gCz)
+        out[name] = {"loss": loss, "dloss_dn": gn, "grad_B_norm": float(np.linalg.norm(gB)),
+                     "forward_s": t1 - t0, "backward_s": t3 - t2,
+                     "backward_cell_steps_per_s": sc.nx * sc.ny * steps / (t3 - t2)}
+    loss, gB, gCz = grads["f64"]
+    out["f32_vs_f64_grad_rel_l2"] = float(np.linalg.norm(grads["f32"][1] - gB) / np.linalg.norm(gB))
+    # central differences on random smooth directions (random Gaussian bumps) and a random n component
+    grid = sc.grid()
+    f = vf.cell_faces(grid, interior=False)
+    rng = np.random.default_rng(20241206)
+    rel = []
+    for k in range(args.adjoint_fd_dirs):
+        v = np.zeros_like(sc.B)
+        for _ in range(3):
+            cx, cy = rng.uniform(0, sc.nx), rng.uniform(0, sc.ny)
+            s = rng.uniform(10.0, 80.0)
+            v += rng.standard_normal() * np.exp(-((f[:, :, 0] - cx) ** 2 + (f[:, :, 1] - cy) ** 2) / (2 * s * s))
+        vn = float(rng.standard_normal()) * 1e-3
+        eps = 1e-7
+        n0 = sc.manning_n
+        lp = AD.gauge_loss(sc, np.float64, gauges, target, dts, B=sc.B + eps * v, manning_n=n0 + eps * vn)
+        lm = AD.gauge_loss(sc, np.float64, gauges, target, dts, B=sc.B - eps * v, manning_n=n0 - eps * vn)
+        fd = (lp - lm) / (2 * eps)
+        got = float(np.sum(gB * v)) + gCz * 2 * n0 * vn
+        rel.append(abs(fd - got) / max(abs(got), 1e-300))
+    rel = np.array(rel)
+    out["fd"] = {"directions": len(rel), "eps": 1e-7, "rel_err_median": float(np.median(rel)),
+                 "rel_err_p90": float(np.percentile(rel, 90)), "rel_err_max": float(rel.max()),
+                 "within_1e-6": int((rel <= 1e-6).sum()),
+                 "directions_kind": "sums of 3 random Gaussian bumps (width U[10,80] m) on B plus a random n component"}
+    # the oracle on dual numbers (the reference CPU path through ForwardDiff's stand-in)
+    if args.adjoint_dual_dirs > 0:
+        o = bench_oracle_sim(sc)
+        drel = []
+        t0 = time.perf_counter()
+        for k in range(args.adjoint_dual_dirs):
+            v = rng.standard_normal(sc.B.shape)
+            cz = float(rng.standard_normal()) * 1e-3
+            lo, dlo = O.dual_gauge_loss(o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target, Bdot=v, Cz_dot=cz)
+            got = float(np.sum(gB * v)) + gCz * cz
+            drel.append(abs(got - dlo) / abs(dlo))
+        out["dual_oracle"] = {"directions": len(drel), "rel_err_max": float(max(drel)),
+                              "loss_equal": bool(lo == loss), "seconds": time.perf_counter() - t0,
+                              "directions_kind": "white-noise B directions and a random Cz component"}
+    return out
+
+
+def bench_oracle_sim(sc):
+    """The oracle built from a scenario (sources, friction) for the dual-number check."""
+    from oracle import vf_oracle as O
+    src = [(O.SRC_BOTTOM, 0.0)]
+    if sc.rain_m_per_h is not None:
+        src.append((O.SRC_CONST_RAIN, sc.rain_m_per_h))
+    if sc.infiltration_m_per_s is not None:
+        src.append((O.SRC_CONST_INFIL, sc.infiltration_m_per_s))
+    o = O.OracleSim(nx=sc.nx, ny=sc.ny, extent=sc.extent, real_bytes=8, theta=sc.theta, sources=src,
+                    friction=O.FRICTION_BSA2012, friction_Cz=sc.manning_n ** 2, stepper=O.STEPPER_RK2, cfl=sc.cfl,
+                    B=sc.B, **sc.eq)
+    o.set_interior(sc.w0, sc.hu0, sc.hv0)
+    return o
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -588,6 +691,9 @@ def main():
         ens = measure_ensemble(args, local)
     if rank == 0 and world == 1 and args.serving:
         serving = measure_serving(args, local)
+    adjoint = None
+    if rank == 0 and world == 1 and args.adjoint:
+        adjoint = measure_adjoint(args, local)
     if rank != 0:
         return
     head = results[args.dtype]
@@ -604,6 +710,7 @@ def main():
         "variants": {k: v for k, v in results.items() if k != args.dtype},
         "ensemble": ens,
         "serving": serving,
+        "adjoint": adjoint,
     }
     print(json.dumps(line), flush=True)
 

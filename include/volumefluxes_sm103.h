@@ -276,6 +276,39 @@ int vf_server_stats(vf_server* s, int64_t* used_bytes, int32_t* queued, int32_t*
 int vf_server_destroy(vf_server* s);
 const char* vf_server_last_error(vf_server* s);
 
+/* ---- Differentiation -------------------------------------------------------
+ * Reverse-mode gradients of a gauge loss with a frozen dt sequence. The
+ * reference differentiates through its CPU path with ForwardDiff dual numbers
+ * (test/test_swe_ad.jl, examples/optimization.jl); these calls replace that
+ * for large parameter counts: one reverse sweep gives dLoss/dB for every
+ * bottom corner and dLoss/dCz at once. Covered: RungeKutta2,
+ * LinearReconstruction, WallBC, a BottomTopography2D, SourceTermBottom,
+ * ConstantRain, ConstantInfiltration and any ImplicitFriction law. At kinks
+ * (minmod switches, dry faces, the dry clamp) the gradient is the
+ * derivative of the branch the forward pass took. */
+
+/* One step with exactly this dt (no CFL limit): the forward pass with a frozen
+ * dt sequence. t is the simulator's time (time-dependent sources). */
+int vf_step_fixed(vf_handle* h, double dt, double t);
+
+typedef struct vf_adjoint vf_adjoint;
+
+/* Takes the handle's current state as U^0 of an n_steps run; checkpoints every
+ * checkpoint_every steps (<= 0: round(sqrt(n_steps))). */
+int vf_adjoint_create(vf_handle* h, int32_t n_steps, int32_t checkpoint_every, vf_adjoint** out);
+/* Runs the n_steps from U^0 on the handle, keeping checkpoints: with
+ * frozen_dts (n_steps values) as given, else with the CFL dt of every step,
+ * written to dts_out (may be NULL). Leaves the handle at U^n_steps. */
+int vf_adjoint_forward(vf_adjoint* a, const double* frozen_dts, double* dts_out);
+/* loss = sum_g (w[gauge_i[g], gauge_j[g]] - target[g])^2 over interior cells
+ * (0-based) of the final state, and its gradient: grad_B receives
+ * dLoss/dB for every corner, (nx+2gc+1) x (ny+2gc+1) doubles, x fastest;
+ * *grad_Cz receives dLoss/dCz. Any output may be NULL. */
+int vf_adjoint_backward(vf_adjoint* a, const int32_t* gauge_i, const int32_t* gauge_j, const double* target,
+                        int32_t n_gauges, double* loss_out, double* grad_B, double* grad_Cz);
+void vf_adjoint_destroy(vf_adjoint* a);
+const char* vf_adjoint_last_error(vf_adjoint* a);
+
 /* Largest interior row count vf_water_volume_static accepts. */
 #define VF_STATIC_MAX_ROWS 16384
 

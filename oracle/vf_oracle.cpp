@@ -38,16 +38,59 @@
 namespace {
 
 // ---------------------------------------------------------------------------
+// Forward-mode dual number (value, derivative along one direction): the
+// oracle instantiated on it stands in for ForwardDiff through the reference
+// CPU path. Values are computed with exactly the double operations of the
+// double oracle, so every branch is taken as in the double run; the
+// derivative follows the taken branch (the subgradient at kinks).
+struct Dual {
+  double v, d;
+  Dual() : v(0), d(0) {}
+  Dual(double x) : v(x), d(0) {}  // NOLINT: constants and promoted inputs carry no derivative
+  Dual(double x, double dx) : v(x), d(dx) {}
+  explicit operator double() const { return v; }
+  explicit operator float() const { return (float)v; }
+};
+inline Dual operator+(Dual a, Dual b) { return Dual(a.v + b.v, a.d + b.d); }
+inline Dual operator-(Dual a, Dual b) { return Dual(a.v - b.v, a.d - b.d); }
+inline Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
+inline Dual operator*(Dual a, Dual b) { return Dual(a.v * b.v, a.d * b.v + a.v * b.d); }
+inline Dual operator/(Dual a, Dual b) {
+  const double q = a.v / b.v;
+  return Dual(q, (a.d - q * b.d) / b.v);
+}
+inline bool operator<(Dual a, Dual b) { return a.v < b.v; }
+inline bool operator>(Dual a, Dual b) { return a.v > b.v; }
+inline bool operator==(Dual a, Dual b) { return a.v == b.v; }
+inline bool operator!=(Dual a, Dual b) { return a.v != b.v; }
+
+// Math helpers with a Dual overload each.
+inline bool vsignbit(double x) { return std::signbit(x); }
+inline bool vsignbit(float x) { return std::signbit(x); }
+inline bool vsignbit(Dual x) { return std::signbit(x.v); }
+inline double vabs(double x) { return std::fabs(x); }
+inline float vabs(float x) { return std::fabs(x); }
+inline Dual vabs(Dual x) { return Dual(std::fabs(x.v), std::signbit(x.v) ? -x.d : x.d); }
+inline double vsqrt(double x) { return std::sqrt(x); }
+inline float vsqrt(float x) { return std::sqrt(x); }
+inline Dual vsqrt(Dual x) {
+  const double r = std::sqrt(x.v);
+  return Dual(r, r > 0 ? x.d / (2 * r) : 0.0);
+}
+inline double vsign1(double x) { return std::copysign(1.0, x); }
+inline float vsign1(float x) { return std::copysign(1.0f, x); }
+inline Dual vsign1(Dual x) { return Dual(std::copysign(1.0, x.v), 0.0); }
+
 // Julia's IEEE min/max: NaN-propagating, and -0.0 < +0.0.
 template <typename T>
 inline T jl_max(T x, T y) {
   if (x != x || y != y) return x - y;
-  return (x > y || (x == y && !std::signbit(x))) ? x : y;
+  return (x > y || (x == y && !vsignbit(x))) ? x : y;
 }
 template <typename T>
 inline T jl_min(T x, T y) {
   if (x != x || y != y) return x - y;
-  return (x < y || (x == y && std::signbit(x))) ? x : y;
+  return (x < y || (x == y && vsignbit(x))) ? x : y;
 }
 
 // ---------------------------------------------------------------------------
@@ -126,6 +169,10 @@ double cr_cbrt(double x) {
 }
 
 inline float cr_cbrt(float x) { return (float)cr_cbrt((double)x); }
+inline Dual cr_cbrt(Dual x) {
+  const double r = cr_cbrt(x.v);
+  return Dual(r, x.v != 0 ? x.d * r / (3 * x.v) : 0.0);
+}
 
 // ---------------------------------------------------------------------------
 // Deterministic exp for HortonInfiltration: Cody-Waite reduction by ln 2 (split
@@ -171,7 +218,7 @@ struct Sim {
   int N1, N2;          // total cells per direction
   size_t plane;        // N1*N2
   double dx, dy;       // grid spacing, Float64 as in src/grid.jl:82-90
-  std::vector<double> B;  // corners (N1+1)*(N2+1), Float64
+  std::vector<T> B;    // corners (N1+1)*(N2+1), in the real type
   // State buffers U[0..nsub]; left/right face buffers; wavespeed scalar field.
   std::vector<std::vector<T>> U;
   std::vector<T> left, right, ws;
@@ -179,8 +226,9 @@ struct Sim {
   std::vector<T> src_field[VFO_MAX_SOURCES];  // Horton factor or rain field, total grid
   double t;
   double current_dt;
+  double force_dt = -1;  // >= 0: every step uses this dt (frozen dt sequence)
   // Equation constants in the state's real type.
-  T g, rho, cutoff, kappa, theta, cfl;
+  T g, rho, cutoff, kappa, theta, cfl, Cz;
 
   size_t id(int i, int j) const { return (size_t)i + (size_t)N1 * (size_t)j; }
 };
@@ -195,29 +243,29 @@ struct Ops {
   T Bc(int i, int j) const {
     if (s.p.bottom_is_constant) return (T)s.p.bottom_constant;
     const int W = s.N1 + 1;
-    const double* B = s.B.data();
-    return (T)(0.25 * (B[i + W * j] + B[i + 1 + W * j] + B[i + W * (j + 1)] + B[i + 1 + W * (j + 1)]));
+    const T* B = s.B.data();
+    return (T)0.25 * (((B[i + W * j] + B[i + 1 + W * j]) + B[i + W * (j + 1)]) + B[i + 1 + W * (j + 1)]);
   }
   T Bl(int i, int j, int dir) const {
     if (s.p.bottom_is_constant) return (T)s.p.bottom_constant;
     const int W = s.N1 + 1;
-    const double* B = s.B.data();
-    if (dir == 0) return (T)(0.5 * (B[i + W * j] + B[i + W * (j + 1)]));
-    return (T)(0.5 * (B[i + W * j] + B[i + 1 + W * j]));
+    const T* B = s.B.data();
+    if (dir == 0) return (T)0.5 * (B[i + W * j] + B[i + W * (j + 1)]);
+    return (T)0.5 * (B[i + W * j] + B[i + 1 + W * j]);
   }
   T Br(int i, int j, int dir) const {
     if (s.p.bottom_is_constant) return (T)s.p.bottom_constant;
     const int W = s.N1 + 1;
-    const double* B = s.B.data();
-    if (dir == 0) return (T)(0.5 * (B[i + 1 + W * j] + B[i + 1 + W * (j + 1)]));
-    return (T)(0.5 * (B[i + W * (j + 1)] + B[i + 1 + W * (j + 1)]));
+    const T* B = s.B.data();
+    if (dir == 0) return (T)0.5 * (B[i + 1 + W * j] + B[i + 1 + W * (j + 1)]);
+    return (T)0.5 * (B[i + W * (j + 1)] + B[i + 1 + W * (j + 1)]);
   }
 
   // --- src/equations/equation.jl:40-67 -------------------------------------
   T desing(T h) const {
     const T k = s.kappa;
     T m = jl_min<T>(h * h / ((T)2 * k) + k / (T)2.0, k);
-    return std::copysign((T)1, h) * jl_max<T>(std::fabs(h), m);
+    return vsign1(h) * jl_max<T>(vabs(h), m);
   }
 
   // --- src/equations/swe_2D.jl:43-65 ---------------------------------------
@@ -241,8 +289,8 @@ struct Ops {
   void eigen(int dir, const T* q, T* e) const {
     const T h = q[0];
     const T u = (dir == 0 ? q[1] : q[2]) / desing(h);
-    e[0] = u + std::sqrt(s.g * h);
-    e[1] = u - std::sqrt(s.g * h);
+    e[0] = u + vsqrt(s.g * h);
+    e[1] = u - vsqrt(s.g * h);
     e[2] = u;
   }
 
@@ -260,7 +308,7 @@ struct Ops {
     }
     const T aplus = jl_max<T>(jl_max<T>(ep[0], em[0]), (T)0);
     const T aminus = jl_min<T>(jl_min<T>(ep[1], em[1]), (T)0);
-    if (std::fabs(aplus - aminus) < s.kappa) {
+    if (vabs(aplus - aminus) < s.kappa) {
       F[0] = F[1] = F[2] = 0;
       return 0;
     }
@@ -269,7 +317,7 @@ struct Ops {
              ((aplus * aminus) / (aplus - aminus)) * (fplus[k] - fminus[k]);
     }
     if (fminus[0] < s.cutoff && fplus[0] < s.cutoff) return 0;
-    return jl_max<T>(std::fabs(aplus), std::fabs(aminus));
+    return jl_max<T>(vabs(aplus), vabs(aminus));
   }
 
   // --- src/reconstruction/linearreconstruction.jl:28-43 --------------------
@@ -414,7 +462,7 @@ struct Ops {
   // HortonInfiltration, src/sourceterms/source_term_infiltration.jl:68-70,83-88
   void horton(std::vector<T>& out, int n, double t) {
     const T fc = (T)s.p.source_rate[n], f0 = (T)s.p.source_aux[n][0], k = (T)s.p.source_aux[n][1];
-    const T decay = (T)det_exp((double)(-k * (T)t));
+    const T decay = (T)det_exp((double)(-k * (T)t));  // constants only: no derivative
     const T rate = fc + (f0 - fc) * decay;
     const std::vector<T>& f = s.src_field[n];
     const size_t m = s.plane;
@@ -468,7 +516,7 @@ struct Ops {
     }
   }
   void implicit_friction(std::vector<T>& out, const std::vector<T>& prev, double dt) {
-    const T Cz = (T)s.p.friction_Cz;
+    const T Cz = s.Cz;
     const T tdt = (T)dt;
 #pragma omp parallel for schedule(static)
     for (int j = 0; j < s.N2; ++j) {
@@ -476,7 +524,7 @@ struct Ops {
         const T h_star = desing(at(prev, 0, i, j) - Bc(i, j));
         const T u = at(prev, 1, i, j) / h_star;
         const T v = at(prev, 2, i, j) / h_star;
-        T speed = std::sqrt(u * u + v * v);
+        T speed = vsqrt(u * u + v * v);
         if (speed == 0) speed = 0;
         const T S = friction_law(Cz, h_star, speed);
         const T ff[3] = {(T)0, S, S};
@@ -556,7 +604,9 @@ struct Ops {
     std::fill(out.begin(), out.end(), (T)0);
     T speed[2];
     add_time_derivative(out, cur, speed, s.t);
-    if (s_idx == 0) {
+    if (s_idx == 0 && s.force_dt >= 0) {
+      dt = s.force_dt;
+    } else if (s_idx == 0) {
       // timestep_computer, src/simulator.jl:147-150
       const double dxs = s.dx / (double)speed[0];
       const double dys = s.dy / (double)speed[1];
@@ -614,7 +664,7 @@ Sim<T>* make_sim(const vfo_params* p, const double* Bc) {
   s->t = 0;
   s->current_dt = 0;
   s->g = (T)p->g; s->rho = (T)p->rho; s->cutoff = (T)p->depth_cutoff; s->kappa = (T)p->desingularizing_kappa;
-  s->theta = (T)p->theta; s->cfl = (T)p->cfl;
+  s->theta = (T)p->theta; s->cfl = (T)p->cfl; s->Cz = (T)p->friction_Cz;
   return s;
 }
 
@@ -836,6 +886,34 @@ int vfo_update_bc_periodic(double* state, int nx, int ny, int gc) {
   std::vector<double> d(state, state + 3 * s.plane);
   Ops<double>(s).update_bc(d);
   std::memcpy(state, d.data(), 3 * s.plane * sizeof(double));
+  return 0;
+}
+
+int vfo_dual_gauge_loss(const vfo_params* p, const double* B, const double* Bdot, double Cz_dot, const double* w,
+                        const double* hu, const double* hv, const double* dts, int n_steps, const int* gauge_i,
+                        const int* gauge_j, const double* target, int n_gauges, double* loss, double* dloss) {
+  if (check_params(p, B) || !loss || n_steps < 0 || (n_steps > 0 && !dts) || n_gauges < 0) return -1;
+  if (p->real_bytes != 8) return -1;
+  Sim<Dual>* s = make_sim<Dual>(p, B);
+  if (!s) return -2;
+  if (Bdot && !p->bottom_is_constant)
+    for (size_t c = 0; c < s->B.size(); ++c) s->B[c].d = Bdot[c];
+  s->Cz.d = Cz_dot;
+  set_interior(s, w, hu, hv);
+  Ops<Dual> ops(*s);
+  for (int k = 0; k < n_steps; ++k) {
+    s->force_dt = dts[k];
+    ops.perform_step(std::numeric_limits<double>::infinity());
+  }
+  Dual L(0.0);
+  const int gc = p->gc;
+  for (int g = 0; g < n_gauges; ++g) {
+    const Dual x = s->U[0][s->id(gauge_i[g] + gc, gauge_j[g] + gc)] - Dual(target[g]);
+    L = L + x * x;
+  }
+  *loss = L.v;
+  if (dloss) *dloss = L.d;
+  delete s;
   return 0;
 }
 

@@ -102,6 +102,15 @@ int vfo_update_bc_periodic(double* state, int nx, int ny, int gc);
 double vfo_cbrt(double x);
 double vfo_desingularize(double h, double kappa);
 
+/* Float64 dual-number run (the stand-in for ForwardDiff through this path):
+ * from the given interior state, n_steps steps with the frozen dt sequence
+ * dts, bottom corners B + eps*Bdot (Bdot may be NULL) and friction Cz +
+ * eps*Cz_dot; returns loss = sum over gauges of (w[i,j] - target)^2 (interior
+ * 0-based indices) and d loss / d eps. */
+int vfo_dual_gauge_loss(const vfo_params* p, const double* B, const double* Bdot, double Cz_dot, const double* w,
+                        const double* hu, const double* hv, const double* dts, int n_steps, const int* gauge_i,
+                        const int* gauge_j, const double* target, int n_gauges, double* loss, double* dloss);
+
 #ifdef __cplusplus
 }
 #endif

@@ -75,6 +75,8 @@ def load():
         "vfo_set_source_field": (C.c_int, [P, C.c_int, P]),
         "vfo_update_bc_periodic": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
         "vfo_desingularize": (D, [D, D]),
+        "vfo_dual_gauge_loss": (C.c_int, [C.POINTER(Params), P, P, D, P, P, P, P, C.c_int, P, P, P, C.c_int,
+                                          C.POINTER(D), C.POINTER(D)]),
     }
     for n, (r, a) in sig.items():
         f = getattr(lib, n)
@@ -123,6 +125,7 @@ class OracleSim:
             self._B = np.ascontiguousarray(B.T)
             p.bottom_is_constant = 0
             bptr = _p(self._B)
+        self.p = p
         h = C.c_void_p()
         rc = self.lib.vfo_create(C.byref(p), bptr, C.byref(h))
         if rc != 0:
@@ -190,3 +193,31 @@ class OracleSim:
 
 def set_threads(n: int) -> int:
     return load().vfo_set_threads(int(n))
+
+
+def dual_gauge_loss(sim: OracleSim, w, hu, hv, dts, gauges, target, *, B=None, Bdot=None, Cz=None, Cz_dot=0.0):
+    """Loss sum_g (w[g] - target[g])^2 after len(dts) steps with the frozen dt
+    sequence, from the interior state (w, hu, hv) ((nx, ny) arrays), in Float64
+    dual numbers through the oracle with sim's configuration: returns (loss,
+    d loss along (Bdot, Cz_dot)). B / Cz override sim's bottom corners
+    ((N1+1, N2+1), [i, j]) and friction coefficient; gauges: (n, 2) interior
+    indices [i, j]."""
+    lib = sim.lib
+    p = Params()
+    C.pointer(p)[0] = sim.p
+    if Cz is not None:
+        p.friction_Cz = float(Cz)
+    Bt = sim._B if B is None else np.ascontiguousarray(np.asarray(B, dtype=np.float64).T)
+    Bd = None if Bdot is None else np.ascontiguousarray(np.asarray(Bdot, dtype=np.float64).T)
+    arrs = [np.ascontiguousarray(np.asarray(a, dtype=np.float64).T) for a in (w, hu, hv)]
+    d = np.ascontiguousarray(dts, dtype=np.float64)
+    g = np.asarray(gauges, dtype=np.int32)
+    gi, gj = np.ascontiguousarray(g[:, 0]), np.ascontiguousarray(g[:, 1])
+    tg = np.ascontiguousarray(target, dtype=np.float64)
+    loss, dloss = C.c_double(), C.c_double()
+    rc = lib.vfo_dual_gauge_loss(C.byref(p), _p(Bt), None if Bd is None else _p(Bd), float(Cz_dot), _p(arrs[0]),
+                                 _p(arrs[1]), _p(arrs[2]), _p(d), len(d), _p(gi), _p(gj), _p(tg), len(tg),
+                                 C.byref(loss), C.byref(dloss))
+    if rc != 0:
+        raise ValueError(f"oracle dual run failed ({rc})")
+    return loss.value, dloss.value

@@ -1,0 +1,113 @@
+"""Reverse-mode gradients on the GPU (vf_adjoint_*): dLoss/dB for every bottom
+corner and dLoss/dCz of the gauge loss sum_g (w_g - target_g)^2, with the dt
+sequence frozen from the forward pass, checked against the oracle run on
+dual numbers (the stand-in for ForwardDiff through the reference CPU path)
+and against central finite differences."""
+import math
+
+import numpy as np
+import pytest
+
+import volumefluxes_sm103 as vf
+from volumefluxes_sm103 import adjoint as AD
+from volumefluxes_sm103 import scenarios as S
+from oracle import vf_oracle as O
+from vfhelpers import oracle_from
+
+pytestmark = pytest.mark.gpu
+
+
+def small_case(n=40, steps=25):
+    case = S.differentiation_case(n, n_gauges=8)
+    extra = np.array([[0, 5], [n - 1, 20], [7, 0], [n - 2, n - 1], [1, 1]], dtype=np.int32)  # next to the walls
+    gauges = np.concatenate([case.gauges, extra])
+    return case, gauges, steps
+
+
+def run_adjoint(case, gauges, steps, real=np.float64, checkpoint_every=4, dts=None):
+    sc = case.scenario
+    sim = sc.build(vf.SM103Backend(real))
+    adj = AD.GaugeAdjoint(sim, steps, checkpoint_every)
+    dts = adj.forward(dts)
+    target = AD.gauge_values(sc, np.float64, gauges, dts, B=case.B_target)
+    loss, gB, gCz = adj.backward(gauges, target)
+    adj.close()
+    return dts, target, loss, gB, gCz
+
+
+def test_adjoint_equals_the_dual_number_oracle():
+    case, gauges, steps = small_case()
+    dts, target, loss, gB, gCz = run_adjoint(case, gauges, steps)
+    sc = case.scenario
+    o = oracle_from(sc)
+    ref_dts = [o.perform_step(math.inf) for _ in range(steps)]
+    assert list(dts) == ref_dts  # the forward pass is the oracle's, bit for bit
+    rng = np.random.default_rng(11)
+    for k in range(4):
+        v = rng.standard_normal(sc.B.shape)
+        cz = float(rng.standard_normal()) * 1e-3
+        lo, dlo = O.dual_gauge_loss(o.o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target, Bdot=v, Cz_dot=cz)
+        assert lo == loss
+        got = float(np.sum(gB * v)) + gCz * cz
+        assert abs(got - dlo) <= 1e-9 * abs(dlo), (k, got, dlo)
+
+
+def test_checkpoint_interval_does_not_change_the_gradient():
+    case, gauges, steps = small_case(n=32, steps=17)
+    a = run_adjoint(case, gauges, steps, checkpoint_every=1)
+    b = run_adjoint(case, gauges, steps, checkpoint_every=5)
+    c = run_adjoint(case, gauges, steps, checkpoint_every=17)
+    assert a[2] == b[2] == c[2]
+    assert np.array_equal(a[3], b[3]) and np.array_equal(a[3], c[3])
+    assert a[4] == b[4] == c[4]
+
+
+def test_cz_gradient_matches_central_differences():
+    case, gauges, steps = small_case()
+    dts, target, loss, gB, gCz = run_adjoint(case, gauges, steps)
+    n = case.scenario.manning_n
+    Cz = n * n
+    eps = 1e-5 * Cz
+    lp = AD.gauge_loss(case.scenario, np.float64, gauges, target, dts, manning_n=math.sqrt(Cz + eps))
+    lm = AD.gauge_loss(case.scenario, np.float64, gauges, target, dts, manning_n=math.sqrt(Cz - eps))
+    fd = (lp - lm) / (2 * eps)
+    # finite differences also see the minmod switches the perturbation crosses,
+    # so they agree only to ~1e-6; the dual-number check above is the exact one
+    assert abs(fd - gCz) <= 1e-5 * abs(gCz), (fd, gCz)
+
+
+def test_smooth_bottom_direction_matches_central_differences():
+    case, gauges, steps = small_case()
+    dts, target, loss, gB, gCz = run_adjoint(case, gauges, steps)
+    sc = case.scenario
+    grid = sc.grid()
+    f = vf.cell_faces(grid, interior=False)
+    v = np.exp(-((f[:, :, 0] - 17.0) ** 2 + (f[:, :, 1] - 23.0) ** 2) / (2 * 8.0 ** 2))  # a smooth bump
+    eps = 1e-7
+    lp = AD.gauge_loss(sc, np.float64, gauges, target, dts, B=sc.B + eps * v)
+    lm = AD.gauge_loss(sc, np.float64, gauges, target, dts, B=sc.B - eps * v)
+    fd = (lp - lm) / (2 * eps)
+    got = float(np.sum(gB * v))
+    assert abs(fd - got) <= 1e-5 * abs(got), (fd, got)
+
+
+def test_float32_gradient_tracks_float64():
+    case, gauges, steps = small_case()
+    d64 = run_adjoint(case, gauges, steps)
+    d32 = run_adjoint(case, gauges, steps, real=np.float32, dts=d64[0])
+    rel = np.linalg.norm(d32[3] - d64[3]) / np.linalg.norm(d64[3])
+    assert rel < 0.05, rel
+    assert abs(d32[4] - d64[4]) <= 0.05 * abs(d64[4])
+
+
+def test_autograd_function_gives_the_adjoint_gradient():
+    torch = pytest.importorskip("torch")
+    case, gauges, steps = small_case(n=24, steps=10)
+    dts, target, loss, gB, gCz = run_adjoint(case, gauges, steps)
+    B = torch.tensor(case.scenario.B, dtype=torch.float64, requires_grad=True)
+    n = torch.tensor(case.scenario.manning_n, dtype=torch.float64, requires_grad=True)
+    L = AD.GaugeLoss.apply(B, n, case.scenario, np.float64, gauges, target, dts)
+    L.backward()
+    assert float(L.detach()) == loss
+    assert np.array_equal(B.grad.numpy(), gB)
+    assert float(n.grad) == gCz * 2 * case.scenario.manning_n

@@ -1,6 +1,6 @@
 """Build libvfsm103.so, the sm_103a shallow-water step library, in-tree.
 
-Six translation units compile in parallel with nvcc and link into one shared
+Seven translation units compile in parallel with nvcc and link into one shared
 library with the CUDA runtime linked statically:
 
   vf_f64.cu  Float64 kernels, -fmad=false (each operation rounds as in Julia)
@@ -9,6 +9,7 @@ library with the CUDA runtime linked statically:
   vf_noalloc.cu  the allocation-free water-volume entry point
   vf_batch.cu  the batched-ensemble entry points
   vf_server.cu  the serving engine
+  vf_adjoint_host.cu  the reverse sweep (checkpointing, recomputation)
 
 Usage: python volumefluxes.jl_gb300/build_native.py [--force]
 """
@@ -37,6 +38,7 @@ UNITS = {
     "vf_noalloc.cu": [],
     "vf_batch.cu": [],
     "vf_server.cu": [],
+    "vf_adjoint_host.cu": [],
 }
 
 

@@ -599,6 +599,23 @@ int vf_step(vf_handle* h, double max_dt, double t, double* dt_out) {
   return VF_OK;
 }
 
+int vf_step_fixed(vf_handle* h, double dt, double t) {
+  int rc = ensure_ready(h);
+  if (rc) return rc;
+  if (!(dt >= 0)) return fail(h, VF_EINVAL, "dt must be >= 0");
+  reset_record(h);
+  h->rec_h->active[0] = 1;
+  h->rec_h->t[0] = t;
+  h->rec_h->explicit_mode = 1;
+  h->rec_h->force_dt = 1;
+  h->rec_h->forced_dt = dt;
+  if ((rc = push_record(h))) return rc;
+  if ((rc = launch_one_step(h, 0))) return rc;
+  if ((rc = pull_record(h))) return rc;
+  std::swap(h->U[0], h->U[1]);
+  return VF_OK;
+}
+
 int vf_simulate(vf_handle* h, double t0, double endtime, int32_t match_endtime, double maximum_timestep,
                 double stop_time, int64_t max_steps, double* t_out, int64_t* steps_out, double* last_dt_out) {
   int rc = ensure_ready(h);

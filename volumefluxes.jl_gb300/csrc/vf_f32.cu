@@ -24,5 +24,17 @@ cudaError_t launch_ensemble(const EnsItem<float>* items, const int* order, int n
 cudaError_t ensemble_max_clusters_f32(int csize, int variant, int* out) {
   return ensemble_max_clusters_impl<float>(csize, variant, out);
 }
+cudaError_t launch_adj_point(const AdjArgs<float>& a, int* nblocks_out, cudaStream_t st) {
+  return launch_adj_point_impl<float>(a, nblocks_out, st);
+}
+cudaError_t launch_adj_recon(const AdjArgs<float>& a, int dir, cudaStream_t st) {
+  return launch_adj_recon_impl<float>(a, dir, st);
+}
+cudaError_t launch_adj_gather(const AdjArgs<float>& a, cudaStream_t st) { return launch_adj_gather_impl<float>(a, st); }
+cudaError_t launch_adj_corner(const AdjArgs<float>& a, cudaStream_t st) { return launch_adj_corner_impl<float>(a, st); }
+cudaError_t launch_adj_seed(const Geom<float>& g, const float* U, float* lam, const int* gi, const int* gj,
+                            const double* target, int n, double* loss, cudaStream_t st) {
+  return launch_adj_seed_impl<float>(g, U, lam, gi, gj, target, n, loss, st);
+}
 cudaError_t configure_kernels_f32() { return configure_impl<float>(); }
 }  // namespace vf

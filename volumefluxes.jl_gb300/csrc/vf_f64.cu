@@ -25,5 +25,21 @@ cudaError_t launch_ensemble(const EnsItem<double>* items, const int* order, int 
 cudaError_t ensemble_max_clusters_f64(int csize, int variant, int* out) {
   return ensemble_max_clusters_impl<double>(csize, variant, out);
 }
+cudaError_t launch_adj_point(const AdjArgs<double>& a, int* nblocks_out, cudaStream_t st) {
+  return launch_adj_point_impl<double>(a, nblocks_out, st);
+}
+cudaError_t launch_adj_recon(const AdjArgs<double>& a, int dir, cudaStream_t st) {
+  return launch_adj_recon_impl<double>(a, dir, st);
+}
+cudaError_t launch_adj_gather(const AdjArgs<double>& a, cudaStream_t st) { return launch_adj_gather_impl<double>(a, st); }
+cudaError_t launch_adj_corner(const AdjArgs<double>& a, cudaStream_t st) { return launch_adj_corner_impl<double>(a, st); }
+cudaError_t launch_adj_seed(const Geom<double>& g, const double* U, double* lam, const int* gi, const int* gj,
+                            const double* target, int n, double* loss, cudaStream_t st) {
+  return launch_adj_seed_impl<double>(g, U, lam, gi, gj, target, n, loss, st);
+}
+cudaError_t launch_adj_sum(const double* part, int n, double* acc, cudaStream_t st) {
+  k_adj_sum<<<1, 32, 0, st>>>(part, n, acc);
+  return cudaGetLastError();
+}
 cudaError_t configure_kernels_f64() { return configure_impl<double>(); }
 }  // namespace vf

@@ -52,7 +52,8 @@ struct StepRecord {
   long long n_done;
   double explicit_max_dt;
   int explicit_mode;
-  int pad_;
+  int force_dt;        // 1: every step uses forced_dt (a frozen dt sequence)
+  double forced_dt;
 };
 
 template <typename T>
@@ -420,6 +421,7 @@ __device__ __forceinline__ double loop_max_dt(int match_endtime, double endtime,
 // dt and time bookkeeping of the step of this parity.
 template <typename T>
 __device__ __forceinline__ double step_dt(const Geom<T>& g, const StepRecord* rec, int parity) {
+  if (rec->force_dt) return rec->forced_dt;
   const double ax = speed_from_key<T>(rec->speed_bits[parity][0]);
   const double ay = speed_from_key<T>(rec->speed_bits[parity][1]);
   const double max_dt = rec->explicit_mode

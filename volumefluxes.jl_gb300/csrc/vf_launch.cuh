@@ -2,6 +2,7 @@
 // type. The Float64 set lives in vf_f64.cu (built with -fmad=false so every
 // expression rounds as in Julia), the Float32 set in vf_f32.cu.
 #pragma once
+#include "vf_adjoint.cuh"
 #include "vf_ensemble.cuh"
 #include "vf_march.cuh"
 
@@ -44,6 +45,21 @@ cudaError_t launch_ensemble(const EnsItem<float>* items, const int* order, int n
 // Clusters of csize CTAs that fit on the device at once (0: csize not launchable).
 cudaError_t ensemble_max_clusters_f64(int csize, int variant, int* out);
 cudaError_t ensemble_max_clusters_f32(int csize, int variant, int* out);
+// Adjoint kernels (vf_adjoint.cuh), one launch each; *nblocks_out receives the
+// number of dLoss/dCz partials k_adj_point wrote.
+cudaError_t launch_adj_point(const AdjArgs<double>& a, int* nblocks_out, cudaStream_t st);
+cudaError_t launch_adj_point(const AdjArgs<float>& a, int* nblocks_out, cudaStream_t st);
+cudaError_t launch_adj_recon(const AdjArgs<double>& a, int dir, cudaStream_t st);
+cudaError_t launch_adj_recon(const AdjArgs<float>& a, int dir, cudaStream_t st);
+cudaError_t launch_adj_gather(const AdjArgs<double>& a, cudaStream_t st);
+cudaError_t launch_adj_gather(const AdjArgs<float>& a, cudaStream_t st);
+cudaError_t launch_adj_corner(const AdjArgs<double>& a, cudaStream_t st);
+cudaError_t launch_adj_corner(const AdjArgs<float>& a, cudaStream_t st);
+cudaError_t launch_adj_seed(const Geom<double>& g, const double* U, double* lam, const int* gi, const int* gj,
+                            const double* target, int n, double* loss, cudaStream_t st);
+cudaError_t launch_adj_seed(const Geom<float>& g, const float* U, float* lam, const int* gi, const int* gj,
+                            const double* target, int n, double* loss, cudaStream_t st);
+cudaError_t launch_adj_sum(const double* part, int n, double* acc, cudaStream_t st);
 // Opt the big-shared-memory kernels in on the current device (idempotent).
 cudaError_t configure_kernels_f64();
 cudaError_t configure_kernels_f32();

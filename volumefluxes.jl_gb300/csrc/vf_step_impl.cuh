@@ -143,4 +143,47 @@ cudaError_t launch_volume_impl(const Geom<T>& g, const T* U, const T* B, double*
   return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_adj_point_impl(const AdjArgs<T>& a, int* nblocks_out, cudaStream_t st) {
+  const dim3 blk(32, 8);
+  const dim3 grid((a.g.nx + 31) / 32, (a.g.ny + 7) / 8);
+  k_adj_point<T><<<grid, blk, 0, st>>>(a);
+  if (nblocks_out) *nblocks_out = (int)(grid.x * grid.y);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_adj_recon_impl(const AdjArgs<T>& a, int dir, cudaStream_t st) {
+  const dim3 blk(32, 4);
+  if (dir == 0) {
+    const dim3 grid((a.g.nx + 2 + 31) / 32, (a.g.ny + 3) / 4);
+    k_adj_recon<T, 0><<<grid, blk, 0, st>>>(a);
+  } else {
+    const dim3 grid((a.g.ny + 2 + 31) / 32, (a.g.nx + 3) / 4);
+    k_adj_recon<T, 1><<<grid, blk, 0, st>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_adj_gather_impl(const AdjArgs<T>& a, cudaStream_t st) {
+  const dim3 blk(32, 8);
+  k_adj_gather<T><<<dim3((a.g.nx + 31) / 32, (a.g.ny + 7) / 8), blk, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_adj_corner_impl(const AdjArgs<T>& a, cudaStream_t st) {
+  const dim3 blk(32, 8);
+  k_adj_corner<T><<<dim3((a.g.N1 + 1 + 31) / 32, (a.g.N2 + 1 + 7) / 8), blk, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_adj_seed_impl(const Geom<T>& g, const T* U, T* lam, const int* gi, const int* gj,
+                                 const double* target, int n, double* loss, cudaStream_t st) {
+  k_adj_seed<T><<<1, 32, 0, st>>>(g, U, lam, gi, gj, target, n, loss);
+  return cudaGetLastError();
+}
+
 }  // namespace vf

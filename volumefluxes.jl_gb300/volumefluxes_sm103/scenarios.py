@@ -7,6 +7,12 @@
                        w = max(1.5, B_cell) (dry islands), Manning-type friction
                        n = 0.03 (friction_bsa2012, Cz = n^2), rain 1e-5 m/s,
                        infiltration 2e-6 m/s, wall BCs, RK2, CFL 0.25.
+  differentiation_case the gradient workload: n x n cells, Δ = 1 m, 16 seeded hills
+                       (amplitude U[0.2,1] m, width U[50,200] m) + 1e-3 slope,
+                       uniform initial depth 1 m, Manning n = 0.03 (bsa2012),
+                       rain 2e-5 m/s, wall BCs, RK2, CFL 0.25; 32 seeded gauge
+                       cells; the target comes from the same steps on the
+                       terrain plus a seeded perturbation (8 hills of U[-0.1,0.1] m).
   ensemble_member      one flood scenario of the batched ensemble: square side
                        log-uniform in [64, 1024] cells with Δ = 1 m, 8-32 seeded
                        hills (amplitude U[0.5,4] m, width U[50,400] m, centres in
@@ -228,3 +234,25 @@ def serving_specs(count: int = 48, seed: int = 20241204, side_range=(128, 2048),
         sp.endtime = float(np.float32(rng.uniform(*endtime_range)))
         out.append(ServingSpec(sp, "f32" if rng.uniform() < 0.5 else "f64"))
     return out
+
+
+@dataclass
+class DiffCase:
+    scenario: Scenario
+    gauges: np.ndarray        # (32, 2) interior cell indices [i, j]
+    B_target: np.ndarray      # perturbed corners, the target run's terrain
+
+
+def differentiation_case(n: int = 512, seed: int = 20241205, n_gauges: int = 32, depth: float = 1.0) -> DiffCase:
+    L = float(n)
+    extent = ((0.0, L), (0.0, L))
+    B = hill_bottom(n, n, extent, 16, seed, amp=(0.2, 1.0), width=(50.0, 200.0))
+    pert = hill_bottom(n, n, extent, 8, seed + 1, slope=0.0, amp=(-0.1, 0.1), width=(30.0, 120.0))
+    Bc = 0.25 * (B[:-1, :-1] + B[1:, :-1] + B[:-1, 1:] + B[1:, 1:])[2:-2, 2:-2]
+    w0 = Bc + depth
+    z = np.zeros_like(w0)
+    rng = SplitMix64(seed + 2)
+    gauges = np.array([[int(rng.uniform(0, n)), int(rng.uniform(0, n))] for _ in range(n_gauges)], dtype=np.int32)
+    sc = Scenario(name=f"diff_{n}", nx=n, ny=n, extent=extent, B=B, w0=w0, hu0=z, hv0=z.copy(), cfl=0.25,
+                  rain_m_per_h=2e-5 * 3600, manning_n=0.03, bottom_source=True, meta={"seed": seed})
+    return DiffCase(sc, np.minimum(gauges, n - 1), B + pert)
