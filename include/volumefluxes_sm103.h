@@ -152,6 +152,14 @@ int vf_simulate(vf_handle* h, double t0, double endtime, int32_t match_endtime, 
  * examples/example_tools.jl:49-106). */
 int vf_water_volume(vf_handle* h, double* out);
 
+/* (w, hu, hv) of n interior cells (0-based i, j) of the current state, in the
+ * real type, without downloading the state: the gauge reads a callback such
+ * as an IntervalWriter (src/callbacks.jl:40-55) makes every interval, where
+ * the reference collects the whole interior (examples/example_tools.jl:99).
+ * Any output may be NULL. */
+int vf_sample_cells(vf_handle* h, const int32_t* i, const int32_t* j, int32_t n, void* w_out, void* hu_out,
+                    void* hv_out);
+
 /* Device-resident access for callers that keep data on the GPU: the current
  * state's device base pointer, its row pitch and plane stride in elements,
  * and the element offset of total cell (0, 0). Valid until the next step. */

@@ -99,3 +99,25 @@ def test_kernels_are_the_compute_path():
     vf.simulate_to_time(sim, 0.01)
     assert sim.launch_count() > n0
     assert vf.library_path().name == "libvfsm103.so"
+
+
+def test_sample_cells_reads_gauges_without_a_download():
+    from vfhelpers import hills_rect
+    sim = hills_rect(70, 45).build(vf.SM103Backend())
+    vf.simulate_to_time(sim, 2.0)
+    cells = np.array([[0, 0], [69, 44], [10, 30], [35, 7]])
+    s = vf.sample_cells(sim, cells)
+    full = vf.current_interior_state(sim)
+    for k, (i, j) in enumerate(cells):
+        assert s.h[k] == full.h[i, j] and s.hu[k] == full.hu[i, j] and s.hv[k] == full.hv[i, j]
+    with pytest.raises(vf.ArgumentError):
+        vf.sample_cells(sim, [[70, 0]])
+
+
+def test_gauge_recorder_in_an_interval_writer():
+    from vfhelpers import hills_rect
+    sim = hills_rect(48, 40).build(vf.SM103Backend())
+    rec = vf.GaugeRecorder([[5, 5], [40, 30]])
+    vf.simulate_to_time(sim, 3.0, callback=vf.IntervalWriter(step=1.0, writer=rec))
+    assert len(rec.times) >= 3 and all(v.shape == (2,) for v in rec.values)
+    assert rec.times == sorted(rec.times)

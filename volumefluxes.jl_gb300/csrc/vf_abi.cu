@@ -311,6 +311,8 @@ void destroy(vf_handle* h) {
     dfree(h, h->rec);
     dfree(h, h->partial);
     dfree(h, h->vol_out);
+    dfree(h, h->sample_ij);
+    dfree(h, h->sample_out);
     for (int i = 0; i < VF_MAX_SOURCES; ++i) {
       dfree(h, h->src_field[i]);
       dfree(h, h->src_tab[i]);
@@ -744,6 +746,42 @@ int vf_water_volume(vf_handle* h, double* out) {
   h->launches += 2;
   if (e != cudaSuccess) return cuda_fail(h, e, "volume launch");
   VF_CK(h, cudaMemcpyAsync(out, h->vol_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  VF_CK(h, cudaStreamSynchronize(h->stream));
+  return VF_OK;
+}
+
+int vf_sample_cells(vf_handle* h, const int32_t* i, const int32_t* j, int32_t n, void* w_out, void* hu_out,
+                    void* hv_out) {
+  int rc = ensure_ready(h);
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!i || !j))) return fail(h, VF_EINVAL, "bad gauge list");
+  if (n == 0) return VF_OK;
+  for (int k = 0; k < n; ++k)
+    if (i[k] < 0 || j[k] < 0 || i[k] >= h->cfg.nx || j[k] >= h->cfg.ny) return fail(h, VF_EINVAL, "gauge outside the grid");
+  if (n > h->sample_cap) {
+    dfree(h, h->sample_ij);
+    dfree(h, h->sample_out);
+    h->sample_ij = nullptr;
+    h->sample_out = nullptr;
+    h->sample_cap = 0;
+    if (!dalloc(h, reinterpret_cast<void**>(&h->sample_ij), sizeof(int) * 2 * (size_t)n) ||
+        !dalloc(h, &h->sample_out, h->elem * 3 * (size_t)n))
+      return fail(h, VF_ENOMEM, "device allocation failed");
+    h->sample_cap = n;
+  }
+  VF_CK(h, cudaMemcpyAsync(h->sample_ij, i, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+  VF_CK(h, cudaMemcpyAsync(h->sample_ij + n, j, sizeof(int) * n, cudaMemcpyHostToDevice, h->stream));
+  cudaError_t e = h->elem == 8 ? vf::launch_sample(h->ad.g, static_cast<const double*>(h->U[0]), h->sample_ij, n,
+                                                   static_cast<double*>(h->sample_out), h->stream)
+                               : vf::launch_sample(h->af.g, static_cast<const float*>(h->U[0]), h->sample_ij, n,
+                                                   static_cast<float*>(h->sample_out), h->stream);
+  h->launches += 1;
+  if (e != cudaSuccess) return cuda_fail(h, e, "sample launch");
+  void* outs[3] = {w_out, hu_out, hv_out};
+  for (int k = 0; k < 3; ++k)
+    if (outs[k])
+      VF_CK(h, cudaMemcpyAsync(outs[k], static_cast<char*>(h->sample_out) + (size_t)k * n * h->elem, h->elem * n,
+                               cudaMemcpyDeviceToHost, h->stream));
   VF_CK(h, cudaStreamSynchronize(h->stream));
   return VF_OK;
 }

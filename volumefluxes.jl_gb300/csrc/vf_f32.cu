@@ -36,5 +36,9 @@ cudaError_t launch_adj_seed(const Geom<float>& g, const float* U, float* lam, co
                             const double* target, int n, double* loss, cudaStream_t st) {
   return launch_adj_seed_impl<float>(g, U, lam, gi, gj, target, n, loss, st);
 }
+cudaError_t launch_sample(const Geom<float>& g, const float* U, const int* ij, int n, float* out, cudaStream_t st) {
+  k_sample<float><<<(n + 127) / 128, 128, 0, st>>>(g, U, ij, n, out);
+  return cudaGetLastError();
+}
 cudaError_t configure_kernels_f32() { return configure_impl<float>(); }
 }  // namespace vf

@@ -41,5 +41,9 @@ cudaError_t launch_adj_sum(const double* part, int n, double* acc, cudaStream_t 
   k_adj_sum<<<1, 32, 0, st>>>(part, n, acc);
   return cudaGetLastError();
 }
+cudaError_t launch_sample(const Geom<double>& g, const double* U, const int* ij, int n, double* out, cudaStream_t st) {
+  k_sample<double><<<(n + 127) / 128, 128, 0, st>>>(g, U, ij, n, out);
+  return cudaGetLastError();
+}
 cudaError_t configure_kernels_f64() { return configure_impl<double>(); }
 }  // namespace vf

@@ -33,6 +33,9 @@ struct vf_handle {
   bool have_bottom = false;
   std::string err;
   long long launches = 0;
+  int* sample_ij = nullptr;   // gauge indices and values of vf_sample_cells
+  void* sample_out = nullptr;
+  int sample_cap = 0;
   cudaGraphExec_t chunk_exec = nullptr;  // captured chunk of steps (wide batch members)
   int chunk_k = 0;                        // its step count; 0: recapture
   void* chunk_u0 = nullptr;               // U[0] when captured (the buffers swap between calls)

@@ -691,6 +691,17 @@ __global__ void k_bc(Geom<T> g, T* __restrict__ U) {
   }
 }
 
+// State of n interior cells (0-based (i, j) pairs) gathered into out[3][n].
+template <typename T>
+__global__ void k_sample(Geom<T> g, const T* __restrict__ U, const int* __restrict__ ij, int n, T* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const long long o = sidx(g, g.gc + ij[k], g.gc + ij[n + k]);
+  out[k] = U[o];
+  out[n + k] = U[g.PS + o];
+  out[2 * n + k] = U[2 * g.PS + o];
+}
+
 // Water volume sum((w - B_cell) * dx * dy) over the interior, in Float64:
 // per-block partial sums in a fixed order, then one block sums the partials.
 template <typename T>

@@ -45,6 +45,9 @@ cudaError_t launch_ensemble(const EnsItem<float>* items, const int* order, int n
 // Clusters of csize CTAs that fit on the device at once (0: csize not launchable).
 cudaError_t ensemble_max_clusters_f64(int csize, int variant, int* out);
 cudaError_t ensemble_max_clusters_f32(int csize, int variant, int* out);
+// Gather n interior cells' (w, hu, hv) into out (3 x n).
+cudaError_t launch_sample(const Geom<double>& g, const double* U, const int* ij, int n, double* out, cudaStream_t st);
+cudaError_t launch_sample(const Geom<float>& g, const float* U, const int* ij, int n, float* out, cudaStream_t st);
 // Adjoint kernels (vf_adjoint.cuh), one launch each; *nblocks_out receives the
 // number of dLoss/dCz partials k_adj_point wrote.
 cudaError_t launch_adj_point(const AdjArgs<double>& a, int* nblocks_out, cudaStream_t st);

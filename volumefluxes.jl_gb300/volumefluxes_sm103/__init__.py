@@ -20,6 +20,6 @@ from .api import (  # noqa: F401
     SM103Backend, name, get_available_backends, convert_to_backend,
     System, ConservedSystem, StateView, Simulator, system_config,
     set_current_state, current_state, current_interior_state, current_time, current_timestep,
-    perform_step, water_volume, simulate_to_time, IntervalWriter, MultipleCallbacks,
+    perform_step, water_volume, simulate_to_time, IntervalWriter, MultipleCallbacks, sample_cells, GaugeRecorder,
 )
 from ._native import library_path, load as load_library  # noqa: F401

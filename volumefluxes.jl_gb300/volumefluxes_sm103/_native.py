@@ -35,7 +35,7 @@ EXPORTED_SYMBOLS = (
     "vf_server_create", "vf_server_submit", "vf_server_poll", "vf_server_result", "vf_server_timing",
     "vf_server_release",
     "vf_server_stats", "vf_server_destroy", "vf_server_last_error",
-    "vf_step_fixed", "vf_adjoint_create", "vf_adjoint_forward", "vf_adjoint_backward", "vf_adjoint_destroy",
+    "vf_sample_cells", "vf_step_fixed", "vf_adjoint_create", "vf_adjoint_forward", "vf_adjoint_backward", "vf_adjoint_destroy",
     "vf_adjoint_last_error",
 )
 VF_BATCH_OK, VF_BATCH_TIMEOUT, VF_BATCH_STALLED, VF_BATCH_MAX_STEPS = 0, 1, 2, 3
@@ -150,6 +150,7 @@ def load(build_if_missing: bool = False):
                                       C.POINTER(C.c_int64)]),
         "vf_server_destroy": (C.c_int, [C.c_void_p]),
         "vf_server_last_error": (C.c_char_p, [C.c_void_p]),
+        "vf_sample_cells": (C.c_int, [H, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
         "vf_step_fixed": (C.c_int, [H, C.c_double, C.c_double]),
         "vf_adjoint_create": (C.c_int, [H, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
         "vf_adjoint_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),

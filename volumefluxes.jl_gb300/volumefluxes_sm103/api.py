@@ -738,6 +738,32 @@ def water_volume(simulator: Simulator) -> float:
 
 
 # --------------------------------------------------------------------------- callbacks
+def sample_cells(simulator: Simulator, cells) -> StateView:
+    """(w, hu, hv) at the given interior cells ((n, 2) array of 0-based [i, j])
+    read on the device: a gauge read without collecting the whole interior."""
+    g = np.ascontiguousarray(np.asarray(cells, dtype=np.int32).reshape(-1, 2))
+    gi, gj = np.ascontiguousarray(g[:, 0]), np.ascontiguousarray(g[:, 1])
+    out = [np.empty(len(g), dtype=simulator.dtype) for _ in range(3)]
+    lib = simulator._lib
+    N.check(lib, simulator.handle, lib.vf_sample_cells(simulator.handle, N.ptr(gi), N.ptr(gj), len(g), N.ptr(out[0]),
+                                                       N.ptr(out[1]), N.ptr(out[2])))
+    return StateView(*out)
+
+
+class GaugeRecorder:
+    """Callback recording (t, w at the gauges) with device-side reads; wrap it in
+    an IntervalWriter to record at fixed intervals (src/callbacks.jl:40-55)."""
+
+    def __init__(self, cells):
+        self.cells = np.asarray(cells, dtype=np.int32).reshape(-1, 2)
+        self.times: list[float] = []
+        self.values: list[np.ndarray] = []
+
+    def __call__(self, t, simulator):
+        self.times.append(float(t))
+        self.values.append(sample_cells(simulator, self.cells).h.copy())
+
+
 class IntervalWriter:
     """IntervalWriter(step, writer), src/callbacks.jl:40-55: calls writer(t, simulator) when t + dt >= current_t."""
 
