@@ -88,6 +88,16 @@ struct Arith<Dual<T>> {
     const T r = A::sqrt_(x.v);
     return D(r, r > (T)0 ? x.d / ((T)2 * r) : (T)0);
   }
+  // Quotients over one divisor: values as the forward's div_by, derivatives of a/b.
+  struct Recip {
+    D b;
+    typename A::Recip R;
+  };
+  static __device__ __forceinline__ Recip recip(D b) { return Recip{b, A::recip(b.v)}; }
+  static __device__ __forceinline__ D div_by(const Recip& R, D a) {
+    const T q = A::div_by(R.R, a.v);
+    return D(q, (a.d - q * R.b.d) / R.b.v);
+  }
   // For equal values the forward max/min may return either operand; these
   // say which, so the derivative follows the same operand.
   static __device__ __forceinline__ bool picks_second_max(T x, T y) {

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include "vf_idiv.cuh"
+#include "vf_sdiv.cuh"
 
 // Float64 division on the integer pipe (1) or the FP64 pipe (0). Both are
 // correctly rounded. Measured on the 4096^2 wet/dry step the integer-pipe
@@ -25,6 +26,15 @@
 // default and the integer path stays as a build option.
 #ifndef VF_FP64_INT_DIV
 #define VF_FP64_INT_DIV 0
+#endif
+// Float64 quotients sharing a divisor through one refined reciprocal and an
+// exact rounding test (1), or one IEEE division each (0); both are exact.
+// Measured on the 4096^2 wet/dry step the shared form was slower (41.6 vs
+// 31.5 ms/step): the hardware division costs about seven FP64 operations, and
+// the rounding test plus its 64-bit integer work outweigh the saved Newton
+// steps, so one division each is the default.
+#ifndef VF_FP64_SHARED_DIV
+#define VF_FP64_SHARED_DIV 0
 #endif
 
 namespace vf {
@@ -76,6 +86,26 @@ struct Arith<double> {
   }
   static __device__ __forceinline__ double rcp(double b) { return 1.0 / b; }
   static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+  // Several quotients over one divisor, each still IEEE a/b (vf_sdiv.cuh).
+  using Recip = SharedRecip;
+  static __device__ __forceinline__ Recip recip(double b) {
+#if VF_FP64_SHARED_DIV
+    return sd_recip(b);
+#else
+    SharedRecip R;
+    R.b = b;
+    R.y = 0.0;
+    R.eb = 0;
+    return R;
+#endif
+  }
+  static __device__ __forceinline__ double div_by(const Recip& R, double a) {
+#if VF_FP64_SHARED_DIV
+    return sd_div(R, a);
+#else
+    return div(a, R.b);
+#endif
+  }
 };
 
 template <>
@@ -92,6 +122,12 @@ struct Arith<float> {
   static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
   static __device__ __forceinline__ float rcp(float b) { return __frcp_rn(b); }
   static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
+  // Quotients over one divisor: one reciprocal, then products.
+  struct Recip {
+    float r;
+  };
+  static __device__ __forceinline__ Recip recip(float b) { return Recip{__frcp_rn(b)}; }
+  static __device__ __forceinline__ float div_by(const Recip& R, float a) { return a * R.r; }
 };
 
 // ---------------------------------------------------------------------------
@@ -291,15 +327,9 @@ template <typename T, int DIR>
 __device__ __forceinline__ void side_flux(const Phys<T>& p, T h, T hu, T hv, T& f0, T& f1, T& f2, T& l1, T& l2) {
   using A = Arith<T>;
   const T hs = desing<T>(h, p.kappa);
-  T u, v;
-  if (A::exact) {
-    u = A::div(hu, hs);
-    v = A::div(hv, hs);
-  } else {
-    const T r = A::rcp(hs);
-    u = hu * r;
-    v = hv * r;
-  }
+  const typename A::Recip R = A::recip(hs);
+  const T u = A::div_by(R, hu);
+  const T v = A::div_by(R, hv);
   const T rh = p.rho * h;
   const T hh = h * h;
   if (DIR == 0) {
@@ -335,18 +365,11 @@ __device__ __forceinline__ void cu_face(const Phys<T>& p, T mh, T mhu, T mhv, T 
     if (SPEED) speed = (T)0;
     return;
   }
-  if (A::exact) {
-    const T q = A::div(aplus * aminus, d);
-    F0 = A::div(aplus * fm0 - aminus * fp0, d) + q * (ph - mh);
-    F1 = A::div(aplus * fm1 - aminus * fp1, d) + q * (phu - mhu);
-    F2 = A::div(aplus * fm2 - aminus * fp2, d) + q * (phv - mhv);
-  } else {
-    const T r = A::rcp(d);
-    const T q = aplus * aminus * r;
-    F0 = (aplus * fm0 - aminus * fp0) * r + q * (ph - mh);
-    F1 = (aplus * fm1 - aminus * fp1) * r + q * (phu - mhu);
-    F2 = (aplus * fm2 - aminus * fp2) * r + q * (phv - mhv);
-  }
+  const typename A::Recip R = A::recip(d);
+  const T q = A::div_by(R, aplus * aminus);
+  F0 = A::div_by(R, aplus * fm0 - aminus * fp0) + q * (ph - mh);
+  F1 = A::div_by(R, aplus * fm1 - aminus * fp1) + q * (phu - mhu);
+  F2 = A::div_by(R, aplus * fm2 - aminus * fp2) + q * (phv - mhv);
   if (SPEED)
     speed = (A::lt(mh, p.cutoff) && A::lt(ph, p.cutoff)) ? (T)0 : A::max(fabs(aplus), fabs(aminus));
 }
@@ -403,15 +426,9 @@ template <typename T>
 __device__ __forceinline__ T friction_factor(const Phys<T>& p, T w, T hu, T hv, T Bc) {
   using A = Arith<T>;
   const T hs = desing<T>(w - Bc, p.kappa);
-  T u, v;
-  if (A::exact) {
-    u = A::div(hu, hs);
-    v = A::div(hv, hs);
-  } else {
-    const T r = A::rcp(hs);
-    u = hu * r;
-    v = hv * r;
-  }
+  const typename A::Recip R = A::recip(hs);
+  const T u = A::div_by(R, hu);
+  const T v = A::div_by(R, hv);
   const T speed = A::sqrt_(u * u + v * v);
   T denom;
   if (p.friction == 1) {          // friction_bsa2012
@@ -431,14 +448,9 @@ __device__ __forceinline__ void apply_friction(T tdt, T S, T& hu, T& hv) {
   using A = Arith<T>;
   if (A::is_zero(S)) return;
   const T den = (T)1 - tdt * S;
-  if (A::exact) {
-    hu = A::div(hu, den);
-    hv = A::div(hv, den);
-  } else {
-    const T r = A::rcp(den);
-    hu = hu * r;
-    hv = hv * r;
-  }
+  const typename A::Recip R = A::recip(den);
+  hu = A::div_by(R, hu);
+  hv = A::div_by(R, hv);
 }
 
 // Dry-cell clamp, src/timestepper/timestepper.jl:41-51.
