@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--ensemble-plain-budget", type=float, default=30.0,
                     help="seconds the sequential plain baseline of the ensemble may spend (it runs a sample)")
     ap.add_argument("--no-autotune", action="store_true", help="ensemble with the library's default granularity")
+    ap.add_argument("--ensemble-wide-cells", type=int, default=None,
+                    help="members with at least this many cells run the whole-grid kernels (default: autotuned)")
     ap.add_argument("--ensemble-endtime-cap", type=float, default=None,
                     help="cap every member's end time (small profiling runs only; the metric uses the full times)")
     ap.add_argument("--serving", action="store_true", help="also measure the serving loop (adds ~2 min)")
@@ -367,6 +369,8 @@ def measure_ensemble(args, local):
         tuned, table = E.autotune(probe, steps=60)
         for p in probe:
             p.close()
+    if args.ensemble_wide_cells is not None:
+        tuned = E.BatchOptions(**{**(tuned.__dict__ if tuned else {}), "wide_cells": args.ensemble_wide_cells})
     sims = [sc.build(be) for sc in scen]
     lib = sims[0]._lib
     n0 = sum(s.launch_count() for s in sims)

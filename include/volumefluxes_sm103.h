@@ -206,7 +206,7 @@ typedef struct vf_batch_options {
                               (8..256); 0: 64, halved down to 8 until every warp has two */
   int64_t wide_cells;      /* members with at least this many interior cells run the plain
                               whole-grid kernels on their own stream instead of a cluster;
-                              0: default (1048576), < 0: never */
+                              0: default (262144), < 0: never */
 } vf_batch_options;
 
 typedef struct vf_batch vf_batch;
@@ -257,8 +257,7 @@ const char* vf_batch_last_error(vf_batch* b);
  * output buffers until it is reported done. */
 typedef struct vf_server vf_server;
 
-/* opt: batch options of every launch (NULL: defaults, except wide_cells, which
- * defaults to 262144 here: requests arrive a few at a time); max_steps <= 0: none. */
+/* opt: batch options of every launch (NULL: defaults); max_steps <= 0: none. */
 int vf_server_create(int32_t device, int64_t hbm_budget_bytes, const vf_batch_options* opt, int64_t max_steps,
                      vf_server** out);
 /* Queues a request; *ticket_out identifies it. VF_ENOMEM if it alone exceeds the budget. */

@@ -11,8 +11,9 @@
 // host memory, so the host sees every simulation finish without synchronising
 // the launch it belongs to.
 //
-// Simulations of at least wide_cells interior cells are "wide": a 16-CTA
-// cluster would leave most of the GPU to them alone, so they run the plain
+// Simulations of at least wide_cells interior cells (default 512^2) are
+// "wide": a 16-CTA cluster would leave most of the GPU to them alone and make
+// them the batch's tail, so they run the plain
 // whole-grid step kernels on their handle's stream instead, as the device loop
 // of vf_simulate, in chunks of kChunk steps captured once as a CUDA graph.
 // kInFlight chunks are kept queued; after each, the step record is copied to pinned
@@ -142,7 +143,7 @@ struct Opts {
 };
 
 Opts resolve(const vf_batch_options* o) {
-  Opts r{16, 16, 600.0, 0, 1LL << 20};
+  Opts r{16, 16, 600.0, 0, 1LL << 18};
   if (o) {
     if (o->wide_cells > 0) r.wide_cells = o->wide_cells;
     if (o->wide_cells < 0) r.wide_cells = LLONG_MAX;

@@ -241,13 +241,9 @@ int vf_server_create(int32_t device, int64_t hbm_budget_bytes, const vf_batch_op
   s->device = device;
   s->budget = (size_t)hbm_budget_bytes;
   s->max_steps = max_steps;
-  // Requests usually arrive a few at a time, so a cluster would leave most of
-  // the GPU idle: members from 512^2 cells up take the whole-grid kernels.
-  s->opt.wide_cells = 1LL << 18;
-  s->has_opt = true;
   if (opt) {
     s->opt = *opt;
-    if (opt->wide_cells == 0) s->opt.wide_cells = 1LL << 18;
+    s->has_opt = true;
   }
   s->t0 = std::chrono::steady_clock::now();
   try {
