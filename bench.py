@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=1000, help="timed RK2 steps (the configuration runs 1000)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--n", type=int, default=4096)
+    ap.add_argument("--n", "--grid", dest="n", type=int, default=4096, help="side of the square grid")
     ap.add_argument("--dtype", choices=("f64", "f32"), default="f64")
     ap.add_argument("--no-variant", action="store_true", help="skip the Float32 variant")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
