@@ -110,7 +110,10 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 // Resident CTAs per SM the ensemble kernel is compiled for: two Float64 CTAs
 // fill the shared memory (2 x 77 KB); Float32 takes three.
-template <typename T> struct EnsBlocks { static constexpr int value = sizeof(T) == 8 ? 2 : 3; };
+#ifndef VF_ENS_BLOCKS_F32
+#define VF_ENS_BLOCKS_F32 3
+#endif
+template <typename T> struct EnsBlocks { static constexpr int value = sizeof(T) == 8 ? 2 : VF_ENS_BLOCKS_F32; };
 
 // VAR 0: column-marching RK2 phases (vf_march.cuh), each warp taking strip
 // segments (strip, seg) = unit % nstrips, unit / nstrips, for units

@@ -265,8 +265,22 @@ __device__ __forceinline__ void flux_march_unit(const Geom<T>& g, const Phys<T>&
   }
 }
 
+// Resident blocks per SM the stage kernel is compiled for. The Float32 kernel
+// otherwise takes 92 registers (five blocks, 20 warps) and waits on memory;
+// at eight blocks (64 registers, a few bytes of spill) the 4096^2 stage pass
+// measured 0.616 instead of 0.755 ms. Float64 (190 registers) is bound by the
+// FP64 pipe and is left alone.
+#ifndef VF_MARCH_STAGE_BLOCKS_F32
+#define VF_MARCH_STAGE_BLOCKS_F32 8
+#endif
+#ifndef VF_MARCH_FLUX_BLOCKS_F32
+#define VF_MARCH_FLUX_BLOCKS_F32 1
+#endif
+template <typename T> struct MarchStageBlocks { static constexpr int value = sizeof(T) == 4 ? VF_MARCH_STAGE_BLOCKS_F32 : 1; };
+template <typename T> struct MarchFluxBlocks { static constexpr int value = sizeof(T) == 4 ? VF_MARCH_FLUX_BLOCKS_F32 : 1; };
+
 template <typename T, int SEG>
-__global__ void __launch_bounds__(MW * MWPB) k_flux_march(Geom<T> g, Phys<T> p, const T* __restrict__ U,
+__global__ void __launch_bounds__(MW * MWPB, MarchFluxBlocks<T>::value) k_flux_march(Geom<T> g, Phys<T> p, const T* __restrict__ U,
                                                           const T* __restrict__ B, T* __restrict__ Lout,
                                                           T* __restrict__ Sout, StepRecord* rec, int parity) {
   if (!rec->active[parity]) return;
@@ -419,7 +433,7 @@ __device__ __forceinline__ void stage_march_unit(const Geom<T>& g, const Phys<T>
 }
 
 template <typename T, int SEG>
-__global__ void __launch_bounds__(MW * MWPB) k_stage_march(Geom<T> g, Phys<T> p, const T* __restrict__ U0,
+__global__ void __launch_bounds__(MW * MWPB, MarchStageBlocks<T>::value) k_stage_march(Geom<T> g, Phys<T> p, const T* __restrict__ U0,
                                                            const T* __restrict__ B, const T* __restrict__ Lin,
                                                            const T* __restrict__ Sin, T* __restrict__ Uo,
                                                            StepRecord* rec, int parity) {
