@@ -61,6 +61,9 @@ extern "C" {
 #define VF_STEPPER_RK2 2      /* RungeKutta2, src/timestepper/rungekutta.jl:21-52 */
 #define VF_BC_WALL 1          /* WallBC, src/bc.jl:81-110 */
 #define VF_BC_PERIODIC 2      /* PeriodicBC, src/bc.jl:29-40 */
+#define VF_BC_NEUMANN 3       /* NeumannBC as src/bc.jl:49-60 computes it: left columns mirror the interior,
+                                 bottom rows copy the top interior rows, right and top ghosts evolve by the
+                                 all-cell passes alone (ghost copied onto ghost) */
 #define VF_REC_LINEAR 1       /* LinearReconstruction(theta), src/reconstruction/linearreconstruction.jl:22-102 */
 #define VF_REC_NONE 2         /* NoReconstruction, src/reconstruction/noreconstruction.jl:30-46 */
 

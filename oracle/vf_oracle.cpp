@@ -569,8 +569,35 @@ struct Ops {
     }
   }
 
+  // --- src/bc.jl:49-60: NeumannBC in 2D, as written. X: left ghosts mirror
+  // the interior; on the right, data[N1-(gc-g)] = data[N1-g+1] copies ghost
+  // onto ghost (g = 1, 2, ... in order). Y: bottom ghosts take the top
+  // interior rows (data[i, N2+g-2gc]); on the top, ghost onto ghost again.
+  // The right and top ghosts therefore keep the values the all-cell passes
+  // give them.
+  void update_bc_neumann(std::vector<T>& d) {
+    const int gc = s.p.gc, N1 = s.N1, N2 = s.N2;
+    for (int j = gc; j < gc + s.p.ny; ++j) {
+      for (int g = 1; g <= gc; ++g) {
+        for (int k = 0; k < 3; ++k) {
+          at(d, k, g - 1, j) = at(d, k, 2 * gc - g, j);
+          at(d, k, N1 - (gc - g) - 1, j) = at(d, k, N1 - g, j);
+        }
+      }
+    }
+    for (int g = 1; g <= gc; ++g) {
+      for (int i = gc; i < gc + s.p.nx; ++i) {
+        for (int k = 0; k < 3; ++k) {
+          at(d, k, i, g - 1) = at(d, k, i, N2 + g - 2 * gc - 1);
+          at(d, k, i, N2 - (gc - g) - 1) = at(d, k, i, N2 - g);
+        }
+      }
+    }
+  }
+
   void update_bc(std::vector<T>& d) {
     if (s.p.bc == VFO_BC_PERIODIC) update_bc_periodic(d);
+    else if (s.p.bc == VFO_BC_NEUMANN) update_bc_neumann(d);
     else update_bc_wall(d);
   }
 
@@ -673,7 +700,7 @@ int check_params(const vfo_params* p, const double* B) {
   if (p->nx < 2 || p->ny < 2 || p->gc < 2) return -1;
   if (p->real_bytes != 8 && p->real_bytes != 4) return -1;
   if (p->stepper != VFO_STEPPER_FE && p->stepper != VFO_STEPPER_RK2) return -1;
-  if (p->bc != VFO_BC_WALL && p->bc != VFO_BC_PERIODIC) return -1;
+  if (p->bc != VFO_BC_WALL && p->bc != VFO_BC_PERIODIC && p->bc != VFO_BC_NEUMANN) return -1;
   if (p->reconstruction != VFO_REC_LINEAR && p->reconstruction != VFO_REC_NONE) return -1;
   if (p->n_sources < 0 || p->n_sources > VFO_MAX_SOURCES) return -1;
   if (!p->bottom_is_constant && !B) return -1;
@@ -881,6 +908,19 @@ int vfo_update_bc_periodic(double* state, int nx, int ny, int gc) {
   Sim<double> s;
   std::memset(&s.p, 0, sizeof(s.p));
   s.p.nx = nx; s.p.ny = ny; s.p.gc = gc; s.p.bc = VFO_BC_PERIODIC;
+  s.N1 = nx + 2 * gc; s.N2 = ny + 2 * gc;
+  s.plane = (size_t)s.N1 * s.N2;
+  std::vector<double> d(state, state + 3 * s.plane);
+  Ops<double>(s).update_bc(d);
+  std::memcpy(state, d.data(), 3 * s.plane * sizeof(double));
+  return 0;
+}
+
+int vfo_update_bc_neumann(double* state, int nx, int ny, int gc) {
+  if (!state || nx < gc || ny < gc || gc < 1) return -1;
+  Sim<double> s;
+  std::memset(&s.p, 0, sizeof(s.p));
+  s.p.nx = nx; s.p.ny = ny; s.p.gc = gc; s.p.bc = VFO_BC_NEUMANN;
   s.N1 = nx + 2 * gc; s.N2 = ny + 2 * gc;
   s.plane = (size_t)s.N1 * s.N2;
   std::vector<double> d(state, state + 3 * s.plane);

@@ -34,7 +34,7 @@ enum {
 
 enum { VFO_FRICTION_NONE = 0, VFO_FRICTION_BSA2012 = 1, VFO_FRICTION_FCG2016 = 2, VFO_FRICTION_BH2021 = 3 };
 enum { VFO_STEPPER_FE = 1, VFO_STEPPER_RK2 = 2 };
-enum { VFO_BC_WALL = 1, VFO_BC_PERIODIC = 2 };
+enum { VFO_BC_WALL = 1, VFO_BC_PERIODIC = 2, VFO_BC_NEUMANN = 3 };
 enum { VFO_REC_LINEAR = 1, VFO_REC_NONE = 2 };
 enum { VFO_MAX_SOURCES = 8 };
 
@@ -99,6 +99,7 @@ double vfo_bottom_lookup(const double* B, int n1p1, int n2p1, int i, int j, int 
 int vfo_update_bc_wall(double* state, int nx, int ny, int gc);
 /* Periodic boundary update in place on a full 3-plane state. */
 int vfo_update_bc_periodic(double* state, int nx, int ny, int gc);
+int vfo_update_bc_neumann(double* state, int nx, int ny, int gc);
 double vfo_cbrt(double x);
 double vfo_desingularize(double h, double kappa);
 

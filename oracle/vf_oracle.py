@@ -15,7 +15,7 @@ HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "libvforacle.so"
 
 SRC_BOTTOM, SRC_CONST_RAIN, SRC_CONST_INFIL, SRC_TIME_RAIN, SRC_HORTON, SRC_RAIN_FIELD = 1, 2, 3, 4, 5, 6
-BC_WALL, BC_PERIODIC = 1, 2
+BC_WALL, BC_PERIODIC, BC_NEUMANN = 1, 2, 3
 REC_LINEAR, REC_NONE = 1, 2
 FRICTION_NONE, FRICTION_BSA2012, FRICTION_FCG2016, FRICTION_BH2021 = 0, 1, 2, 3
 STEPPER_FE, STEPPER_RK2 = 1, 2
@@ -74,6 +74,7 @@ def load():
         "vfo_set_source_table": (C.c_int, [P, C.c_int, P, P, C.c_int]),
         "vfo_set_source_field": (C.c_int, [P, C.c_int, P]),
         "vfo_update_bc_periodic": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
+        "vfo_update_bc_neumann": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
         "vfo_desingularize": (D, [D, D]),
         "vfo_dual_gauge_loss": (C.c_int, [C.POINTER(Params), P, P, D, P, P, P, P, C.c_int, P, P, P, C.c_int,
                                           C.POINTER(D), C.POINTER(D)]),

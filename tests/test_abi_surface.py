@@ -71,7 +71,7 @@ def _cfg(**kw):
 
 
 @pytest.mark.parametrize("bad", [
-    {"gc": 1}, {"nx": 1}, {"real_bytes": 2}, {"stepper": 7}, {"bc": 3}, {"reconstruction": 0}, {"friction": 9},
+    {"gc": 1}, {"nx": 1}, {"real_bytes": 2}, {"stepper": 7}, {"bc": 4}, {"reconstruction": 0}, {"friction": 9},
     {"abi_version": 99}, {"cfl": 0.0}, {"bottom_constant": 1.0}, {"desingularizing_kappa": 0.0},
 ])
 def test_create_rejects_invalid_configurations_without_touching_the_gpu(lib, bad):

@@ -60,11 +60,15 @@ def test_conserved_system_compatibility():
         vf.ShallowWaterEquations(vf.BottomTopography2D(np.ones((8, 9)), vf.SM103Backend(), g))
 
 
-@pytest.mark.parametrize("change", ["neumann", "gc1", "pure_backend"])
+class _OtherBC(vf.BoundaryCondition):
+    pass
+
+
+@pytest.mark.parametrize("change", ["other_bc", "gc1", "pure_backend"])
 def test_unsupported_configurations_raise(change):
     be = vf.SM103Backend()
     g = vf.CartesianGrid(8, 8, gc=1 if change == "gc1" else 2,
-                         boundary=vf.NeumannBC() if change == "neumann" else vf.WallBC())
+                         boundary=_OtherBC() if change == "other_bc" else vf.WallBC())
     eq = vf.ShallowWaterEquations()
     rec = vf.LinearReconstruction()
     sys_ = vf.ConservedSystem(be, rec, vf.CentralUpwind(eq), eq, g)

@@ -42,6 +42,7 @@ MIXED = {
     "dam_break_256": (lambda: S.circular_dam_break(256), 0.02),
     "step_13x7": (lambda: nonsquare_step(13, 7), 0.05),
     "dry_circle_periodic_64": (lambda: dry_circle_periodic(64), 0.02),
+    "hills_neumann_70x45": (lambda: hills_rect(70, 45, bc="neumann"), 2.5),
 }
 
 

@@ -50,6 +50,10 @@ CASES = {
     "time_rain_and_horton_rk2": (lambda: terrain_sources(64, 48), 80),
     "time_rain_and_horton_periodic_fe": (lambda: terrain_sources(45, 33, bc="periodic", stepper="fe"), 80),
     "functional_rain_spatial_fe": (lambda: functional(spatial_rain_fn), 0),
+    "hills_neumann_rk2": (lambda: hills_rect(70, 45, bc="neumann"), 60),
+    "hills_neumann_partial_tiles_fe": (lambda: hills_rect(37, 19, bc="neumann", stepper="fe"), 60),
+    "time_rain_and_horton_neumann_rk2": (lambda: terrain_sources(45, 33, bc="neumann"), 80),
+    "dam_break_neumann_rk2": (lambda: S.Scenario(**{**S.circular_dam_break(64).__dict__, "bc": "neumann"}), 60),
 }
 
 

@@ -186,3 +186,32 @@ def test_no_reconstruction_conserves_mass_on_a_flat_bottom():
         o.perform_step(math.inf)
     h, hu, hv = o.interior()
     assert np.all(np.isfinite(h)) and abs(h.sum() - v0) <= 1e-12 * v0
+
+
+def test_neumann_bc_mapping_as_the_reference_writes_it(lib):
+    # src/bc.jl:49-60 (gc = 2): left columns mirror the interior; right columns
+    # copy ghost onto ghost; bottom rows take the top interior rows; top rows
+    # copy ghost onto ghost. Corners untouched.
+    nx, ny, gc = 9, 7, 2
+    N1, N2 = nx + 2 * gc, ny + 2 * gc
+    rng = np.random.default_rng(3)
+    u = rng.standard_normal((3, N1, N2))
+    buf = np.ascontiguousarray(u.transpose(0, 2, 1)).reshape(-1)
+    assert lib.vfo_update_bc_neumann(buf.ctypes.data, nx, ny, gc) == 0
+    out = buf.reshape(3, N2, N1).transpose(0, 2, 1)
+    I, J = slice(gc, nx + gc), slice(gc, ny + gc)
+    assert np.array_equal(out[:, I, J], u[:, I, J])
+    assert np.array_equal(out[:, 0, J], u[:, 3, J]) and np.array_equal(out[:, 1, J], u[:, 2, J])
+    assert np.array_equal(out[:, N1 - 2, J], u[:, N1 - 1, J]) and np.array_equal(out[:, N1 - 1, J], u[:, N1 - 1, J])
+    assert np.array_equal(out[:, I, 0], u[:, I, N2 - 4]) and np.array_equal(out[:, I, 1], u[:, I, N2 - 3])
+    assert np.array_equal(out[:, I, N2 - 2], u[:, I, N2 - 1]) and np.array_equal(out[:, I, N2 - 1], u[:, I, N2 - 1])
+    assert out[0, 0, 0] == u[0, 0, 0] and out[0, N1 - 1, N2 - 1] == u[0, N1 - 1, N2 - 1]
+
+
+def test_neumann_outflow_runs_and_stays_finite():
+    from vfhelpers import hills_rect
+    o = oracle_from(hills_rect(40, 30, bc="neumann"))
+    for _ in range(30):
+        o.perform_step(math.inf)
+    h, hu, hv = o.interior()
+    assert np.all(np.isfinite(h)) and np.all(np.isfinite(hu)) and np.all(np.isfinite(hv))

@@ -43,7 +43,7 @@ class OracleRun:
         self.o = O.OracleSim(nx=sc.nx, ny=sc.ny, extent=sc.extent, real_bytes=real_bytes, theta=sc.theta,
                              sources=src, friction=fr, friction_Cz=(sc.manning_n ** 2 if sc.manning_n else 0.0),
                              stepper=O.STEPPER_RK2 if sc.stepper == "rk2" else O.STEPPER_FE, cfl=sc.cfl, B=sc.B,
-                             bc=O.BC_PERIODIC if sc.bc == "periodic" else O.BC_WALL,
+                             bc={"periodic": O.BC_PERIODIC, "neumann": O.BC_NEUMANN}.get(sc.bc, O.BC_WALL),
                              reconstruction=O.REC_NONE if sc.reconstruction == "none" else O.REC_LINEAR, **sc.eq)
         for i, (t, r) in tables.items():
             self.o.set_source_table(i, t, r)

@@ -203,8 +203,8 @@ int validate(const vf_config* c) {
     return fail(nullptr, VF_EINVAL, "reconstruction must be LinearReconstruction or NoReconstruction");
   if (c->stepper != VF_STEPPER_FE && c->stepper != VF_STEPPER_RK2)
     return fail(nullptr, VF_EINVAL, "stepper must be ForwardEuler or RungeKutta2");
-  if (c->bc != VF_BC_WALL && c->bc != VF_BC_PERIODIC)
-    return fail(nullptr, VF_EINVAL, "boundary must be WallBC or PeriodicBC");
+  if (c->bc != VF_BC_WALL && c->bc != VF_BC_PERIODIC && c->bc != VF_BC_NEUMANN)
+    return fail(nullptr, VF_EINVAL, "boundary must be WallBC, PeriodicBC or NeumannBC");
   if (!(c->desingularizing_kappa > 0) || !(c->depth_cutoff >= 0))
     return fail(nullptr, VF_EINVAL, "desingularizing_kappa must be positive and depth_cutoff non-negative");
   if (c->friction < VF_FRICTION_NONE || c->friction > VF_FRICTION_BH2021)

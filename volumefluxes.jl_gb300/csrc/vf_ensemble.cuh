@@ -221,14 +221,14 @@ __global__ void __launch_bounds__(NT, EnsBlocks<T>::value) k_ensemble(const EnsI
     } else if constexpr (VAR == 2) {
       for (int tile = (int)rank; tile < ntiles; tile += csize)
         apply_fe_tile<T, true>(g, p, U0, sit.B, sit.L, sit.S, U1, g.gc + (tile % tiles_x) * TX,
-                               g.gc + (tile / tiles_x) * TY, dt);
+                               g.gc + (tile / tiles_x) * TY, dt, t);
     } else {
       for (int tile = (int)rank; tile < ntiles; tile += csize) {
         const int x0 = g.gc + (tile % tiles_x) * TX, y0 = g.gc + (tile / tiles_x) * TY;
         if (sit.rk2) {
           stage2_tile<T, true>(g, p, U0, sit.B, sit.L, sit.S, U1, x0, y0, sm.s, dt, t);
         } else {
-          apply_fe_tile<T, true>(g, p, U0, sit.B, sit.L, sit.S, U1, x0, y0, dt);
+          apply_fe_tile<T, true>(g, p, U0, sit.B, sit.L, sit.S, U1, x0, y0, dt, t);
         }
         __syncthreads();
       }

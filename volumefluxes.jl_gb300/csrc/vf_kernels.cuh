@@ -66,10 +66,13 @@ struct Geom {
   int bc;  // 1 wall (src/bc.jl:81-110), 2 periodic (src/bc.jl:29-40)
 };
 
-// Interior source cell of ghost coordinate v (0 <= v < n + 2gc) along one axis:
-// the mirror for walls, the opposite side for periodic boundaries.
-__device__ __forceinline__ int bc_source(int v, int gc, int n, int bc) {
-  if (bc == 2) return v < gc ? v + n : v - n;
+// Interior source cell of ghost coordinate v (0 <= v < n + 2gc) along axis 0
+// (x) or 1 (y): the mirror for walls (src/bc.jl:81-110), the opposite side for
+// periodic boundaries (src/bc.jl:29-40). NeumannBC as src/bc.jl:49-60 writes
+// it: the left columns mirror the interior, the bottom rows copy the top
+// interior rows; its right and top ghosts have no source (neumann_outer).
+__device__ __forceinline__ int bc_source(int v, int gc, int n, int bc, int axis) {
+  if (bc == 2 || (bc == 3 && axis == 1 && v < gc)) return v < gc ? v + n : v - n;
   return v < gc ? 2 * gc - 1 - v : 2 * (gc + n) - 1 - v;
 }
 
@@ -459,11 +462,16 @@ __device__ __forceinline__ void store_with_ghosts(const Geom<T>& g, T* __restric
   Uo[g.PS + o] = hu;
   Uo[2 * g.PS + o] = hv;
   int gxs[2] = {-1, -1}, gys[2] = {-1, -1};
-  const T sx = g.bc == 2 ? (T)1 : (T)-1;  // momentum sign across an x ghost
+  const T sx = g.bc == 1 ? (T)-1 : (T)1;  // normal momentum sign across a ghost
   if (g.bc == 2) {
     if (gx < 2 * g.gc) gxs[0] = gx + g.nx;
     if (gx >= g.nx) gxs[1] = gx - g.nx;
     if (gy < 2 * g.gc) gys[0] = gy + g.ny;
+    if (gy >= g.ny) gys[1] = gy - g.ny;
+  } else if (g.bc == 3) {  // Neumann: left mirror, bottom from the top rows
+    const int lo = g.gc;
+    if (gx == lo) gxs[0] = lo - 1;
+    if (gx == lo + 1) gxs[0] = lo - 2;
     if (gy >= g.ny) gys[1] = gy - g.ny;
   } else {
     const int lo = g.gc, hi = g.gc + g.nx - 1;
@@ -508,6 +516,58 @@ __device__ __forceinline__ void stage1_point(const Phys<T>& p, T tdt, T u0, T u1
   hv = u2 + tdt * l2;
   if (p.friction) apply_friction<T>(tdt, S, hu, hv);
   dry_clamp<T>(p, w, hu, hv, Bc);
+}
+
+// NeumannBC's right and top ghosts (src/bc.jl:53,58 copy ghost onto ghost):
+// the outer ghost of a row or column evolves by the all-cell passes alone --
+// no flux, its rain and infiltration, its own friction and dry clamp -- and
+// the boundary update copies it onto the inner ghost. (x, y) is the outer
+// ghost; its stage-1 value, and with rk2 its stage-2 value, is written to it
+// and to the inner ghost (x-1, y) or (x, y-1). scal holds point_scalars().
+template <typename T, bool CG>
+__device__ __forceinline__ void neumann_u1(const Geom<T>& g, const Phys<T>& p, T tdt, const T* U0,
+                                           const T* __restrict__ B, const T* scal, int x, int y, T& w, T& hu, T& hv,
+                                           T& a0, T& a1, T& a2, T& lpt, T& Bc) {
+  const long long o = sidx(g, x, y);
+  Bc = g.bconst;
+  if (!g.bottom_const) {
+    const long long b = (long long)y * g.PB + x + XOFF;
+    Bc = (T)0.25 * (((B[b] + B[b + 1]) + B[b + g.PB]) + B[b + g.PB + 1]);
+  }
+  a0 = gld<CG>(U0 + o);
+  a1 = gld<CG>(U0 + g.PS + o);
+  a2 = gld<CG>(U0 + 2 * g.PS + o);
+  lpt = p.any_dynamic ? add_point_sources<T>(p, (T)0, scal, o) : add_point_sources<T>(p, (T)0);
+  T S = (T)0;
+  if (p.friction && friction_active<T>(a1, a2)) S = friction_factor<T>(p, a0, a1, a2, Bc);
+  stage1_point<T>(p, tdt, a0, a1, a2, lpt, (T)0, (T)0, S, Bc, w, hu, hv);
+}
+
+template <typename T, bool CG>
+__device__ __forceinline__ void neumann_outer(const Geom<T>& g, const Phys<T>& p, T tdt, const T* U0,
+                                              const T* __restrict__ B, const T* scal, int x, int y, int axis, bool rk2,
+                                              T* Uo) {
+  T w, hu, hv, a0, a1, a2, lpt, Bc;
+  neumann_u1<T, CG>(g, p, tdt, U0, B, scal, x, y, w, hu, hv, a0, a1, a2, lpt, Bc);
+  if (rk2) {  // src/timestepper/rungekutta.jl:42-50 on the ghost
+    const T v0 = w, v1 = hu, v2 = hv;
+    w = v0 + tdt * lpt;
+    hu = v1 + tdt * (T)0;
+    hv = v2 + tdt * (T)0;
+    w = (T)0.5 * (a0 + w);
+    hu = (T)0.5 * (a1 + hu);
+    hv = (T)0.5 * (a2 + hv);
+    if (p.friction && friction_active<T>(v1, v2)) apply_friction<T>(tdt, friction_factor<T>(p, v0, v1, v2, Bc), hu, hv);
+    dry_clamp<T>(p, w, hu, hv, Bc);
+  }
+  const long long q0 = sidx(g, x, y);
+  const long long q1 = axis == 0 ? sidx(g, x - 1, y) : sidx(g, x, y - 1);
+  Uo[q0] = w;
+  Uo[g.PS + q0] = hu;
+  Uo[2 * g.PS + q0] = hv;
+  Uo[q1] = w;
+  Uo[g.PS + q1] = hu;
+  Uo[2 * g.PS + q1] = hv;
 }
 
 // ---------------------------------------------------------------------------
@@ -560,11 +620,21 @@ __device__ __forceinline__ void stage2_tile(const Geom<T>& g, const Phys<T>& p, 
         s.U0[2 * TX * TY + t] = a2;
       }
     } else if (yin && gx < g.N1) {
-      u1_global<T, CG>(g, p, tdt, U0, Lin, Sin, B, bc_source(gx, g.gc, g.nx, g.bc), gy, w, hu, hv);
-      if (g.bc != 2) hu = -hu;
+      if (g.bc == 3 && gx >= g.gc + g.nx) {
+        T a0, a1, a2, lpt, Bg;
+        neumann_u1<T, CG>(g, p, tdt, U0, B, s.scal, g.N1 - 1, gy, w, hu, hv, a0, a1, a2, lpt, Bg);
+      } else {
+        u1_global<T, CG>(g, p, tdt, U0, Lin, Sin, B, bc_source(gx, g.gc, g.nx, g.bc, 0), gy, w, hu, hv);
+        if (g.bc == 1) hu = -hu;
+      }
     } else if (xin && gy < g.N2) {
-      u1_global<T, CG>(g, p, tdt, U0, Lin, Sin, B, gx, bc_source(gy, g.gc, g.ny, g.bc), w, hu, hv);
-      if (g.bc != 2) hv = -hv;
+      if (g.bc == 3 && gy >= g.gc + g.ny) {
+        T a0, a1, a2, lpt, Bg;
+        neumann_u1<T, CG>(g, p, tdt, U0, B, s.scal, gx, g.N2 - 1, w, hu, hv, a0, a1, a2, lpt, Bg);
+      } else {
+        u1_global<T, CG>(g, p, tdt, U0, Lin, Sin, B, gx, bc_source(gy, g.gc, g.ny, g.bc, 1), w, hu, hv);
+        if (g.bc == 1) hv = -hv;
+      }
     }
     s.U1[idx] = w;
     s.U1[HX * HY + idx] = hu;
@@ -595,6 +665,10 @@ __device__ __forceinline__ void stage2_tile(const Geom<T>& g, const Phys<T>& p, 
     if (p.friction && friction_active<T>(v1, v2)) apply_friction<T>(tdt, friction_factor<T>(p, v0, v1, v2, Bc), hu, hv);
     dry_clamp<T>(p, w, hu, hv, Bc);
     store_with_ghosts<T>(g, Uo, x0 + lx, y0 + ly, w, hu, hv);
+    if (g.bc == 3) {
+      if (x0 + lx == g.gc + g.nx - 1) neumann_outer<T, CG>(g, p, tdt, U0, B, s.scal, g.N1 - 1, y0 + ly, 0, true, Uo);
+      if (y0 + ly == g.gc + g.ny - 1) neumann_outer<T, CG>(g, p, tdt, U0, B, s.scal, x0 + lx, g.N2 - 1, 1, true, Uo);
+    }
   }
 }
 
@@ -623,7 +697,7 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_stage2(Geom<T> g, Ph
 template <typename T, bool CG>
 __device__ __forceinline__ void apply_fe_tile(const Geom<T>& g, const Phys<T>& p, const T* U0,
                                               const T* __restrict__ B, const T* Lin, const T* Sin, T* Uo, int x0,
-                                              int y0, double dt) {
+                                              int y0, double dt, double t) {
   const T tdt = (T)dt;
   const int lx = threadIdx.x % TX, ly0 = threadIdx.x / TX;
   for (int ly = ly0; ly < TY; ly += NT / TX) {
@@ -640,6 +714,12 @@ __device__ __forceinline__ void apply_fe_tile(const Geom<T>& g, const Phys<T>& p
     stage1_point<T>(p, tdt, gld<CG>(U0 + o), gld<CG>(U0 + g.PS + o), gld<CG>(U0 + 2 * g.PS + o), gld<CG>(Lin + o),
                     gld<CG>(Lin + g.PS + o), gld<CG>(Lin + 2 * g.PS + o), S, Bc, w, hu, hv);
     store_with_ghosts<T>(g, Uo, gx, gy, w, hu, hv);
+    if (g.bc == 3 && (gx == g.gc + g.nx - 1 || gy == g.gc + g.ny - 1)) {
+      T scal[8];
+      if (p.any_dynamic) point_scalars<T>(p, t, scal);
+      if (gx == g.gc + g.nx - 1) neumann_outer<T, CG>(g, p, tdt, U0, B, scal, g.N1 - 1, gy, 0, false, Uo);
+      if (gy == g.gc + g.ny - 1) neumann_outer<T, CG>(g, p, tdt, U0, B, scal, gx, g.N2 - 1, 1, false, Uo);
+    }
   }
 }
 
@@ -657,23 +737,34 @@ __global__ void __launch_bounds__(NT) k_apply_fe(Geom<T> g, Phys<T> p, const T* 
   if (threadIdx.x == 0) sdt = step_dt<T>(g, rec, parity);
   __syncthreads();
   const double dt = sdt;
-  apply_fe_tile<T, false>(g, p, U0, B, Lin, Sin, Uo, g.gc + blockIdx.x * TX, g.gc + blockIdx.y * TY, dt);
+  apply_fe_tile<T, false>(g, p, U0, B, Lin, Sin, Uo, g.gc + blockIdx.x * TX, g.gc + blockIdx.y * TY, dt,
+                          rec->t[parity]);
   if (root) advance_record<T>(rec, parity, dt);
 }
 
 // Boundary update of a whole volume (after uploads): wall, src/bc.jl:81-110,
-// or periodic, src/bc.jl:29-40. Ghost columns at interior rows, ghost rows at
-// interior columns; corners untouched.
+// periodic, src/bc.jl:29-40, or Neumann, src/bc.jl:49-60 (right and top: the
+// inner ghost takes the outer ghost's value). Ghost columns at interior rows,
+// ghost rows at interior columns; corners untouched.
 template <typename T>
 __global__ void k_bc(Geom<T> g, T* __restrict__ U) {
   const int n_x = g.ny * 2 * g.gc;
   const int n_y = g.nx * 2 * g.gc;
-  const T sgn = g.bc == 2 ? (T)1 : (T)-1;
+  const T sgn = g.bc == 1 ? (T)-1 : (T)1;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n_x + n_y; idx += gridDim.x * blockDim.x) {
     if (idx < n_x) {
       const int j = g.gc + idx / (2 * g.gc), r = idx % (2 * g.gc);
       const int gx = r < g.gc ? r : g.gc + g.nx + (r - g.gc);
-      const int sx = bc_source(gx, g.gc, g.nx, g.bc);
+      if (g.bc == 3 && gx >= g.gc + g.nx) {
+        if (gx == g.N1 - 2) {
+          const long long d = sidx(g, gx, j), sI = sidx(g, g.N1 - 1, j);
+          U[d] = U[sI];
+          U[g.PS + d] = U[g.PS + sI];
+          U[2 * g.PS + d] = U[2 * g.PS + sI];
+        }
+        continue;
+      }
+      const int sx = bc_source(gx, g.gc, g.nx, g.bc, 0);
       const long long d = sidx(g, gx, j), sI = sidx(g, sx, j);
       U[d] = U[sI];
       U[g.PS + d] = sgn * U[g.PS + sI];
@@ -682,7 +773,16 @@ __global__ void k_bc(Geom<T> g, T* __restrict__ U) {
       const int q = idx - n_x;
       const int i = g.gc + q / (2 * g.gc), r = q % (2 * g.gc);
       const int gy = r < g.gc ? r : g.gc + g.ny + (r - g.gc);
-      const int sy = bc_source(gy, g.gc, g.ny, g.bc);
+      if (g.bc == 3 && gy >= g.gc + g.ny) {
+        if (gy == g.N2 - 2) {
+          const long long d = sidx(g, i, gy), sI = sidx(g, i, g.N2 - 1);
+          U[d] = U[sI];
+          U[g.PS + d] = U[g.PS + sI];
+          U[2 * g.PS + d] = U[2 * g.PS + sI];
+        }
+        continue;
+      }
+      const int sy = bc_source(gy, g.gc, g.ny, g.bc, 1);
       const long long d = sidx(g, i, gy), sI = sidx(g, i, sy);
       U[d] = U[sI];
       U[g.PS + d] = U[g.PS + sI];

@@ -20,7 +20,7 @@ VF_SRC_BOTTOM, VF_SRC_CONST_RAIN, VF_SRC_CONST_INFIL = 1, 2, 3
 VF_SRC_TIME_RAIN, VF_SRC_HORTON, VF_SRC_RAIN_FIELD = 4, 5, 6
 VF_FRICTION_NONE, VF_FRICTION_BSA2012, VF_FRICTION_FCG2016, VF_FRICTION_BH2021 = 0, 1, 2, 3
 VF_STEPPER_FE, VF_STEPPER_RK2 = 1, 2
-VF_BC_WALL, VF_BC_PERIODIC = 1, 2
+VF_BC_WALL, VF_BC_PERIODIC, VF_BC_NEUMANN = 1, 2, 3
 VF_REC_LINEAR, VF_REC_NONE = 1, 2
 
 # Every symbol include/volumefluxes_sm103.h declares.

@@ -532,9 +532,8 @@ def system_config(backend, system: "ConservedSystem", timestepper, grid: Cartesi
         raise ArgumentError(f"{type(s.reconstruction).__name__} is not implemented on the sm_103a backend")
     if not isinstance(s.numericalflux, CentralUpwind):
         raise ArgumentError(f"{type(s.numericalflux).__name__} is not implemented on the sm_103a backend")
-    if not isinstance(g.boundary, (WallBC, PeriodicBC)):
-        raise ArgumentError(f"{type(g.boundary).__name__} is not implemented on the sm_103a backend "
-                            "(WallBC and PeriodicBC are)")
+    if not isinstance(g.boundary, (WallBC, PeriodicBC, NeumannBC)):
+        raise ArgumentError(f"{type(g.boundary).__name__} is not implemented on the sm_103a backend")
     if g.gc != 2:
         raise ArgumentError("the sm_103a backend needs CartesianGrid(...; gc=2)")
     if isinstance(timestepper, RungeKutta2):
@@ -584,7 +583,8 @@ def system_config(backend, system: "ConservedSystem", timestepper, grid: Cartesi
     else:
         raise ArgumentError(f"{type(fr).__name__} is not implemented on the sm_103a backend")
     cfg.stepper = stepper
-    cfg.bc = N.VF_BC_PERIODIC if isinstance(g.boundary, PeriodicBC) else N.VF_BC_WALL
+    cfg.bc = (N.VF_BC_PERIODIC if isinstance(g.boundary, PeriodicBC)
+              else N.VF_BC_NEUMANN if isinstance(g.boundary, NeumannBC) else N.VF_BC_WALL)
     cfg.cfl = float(np.dtype(backend.realtype).type(cfl))
     if isinstance(eq.B, ConstantBottomTopography):
         cfg.bottom_is_constant, cfg.bottom_constant = 1, eq.B.B

@@ -77,7 +77,7 @@ class Scenario:
     bottom_source: bool = False
     friction_law: str = "bsa2012"   # friction_bsa2012 / friction_fcg2016 / friction_bh2021
     eq: dict = field(default_factory=dict)  # ShallowWaterEquations keywords (rho, g, depth_cutoff, ...)
-    bc: str = "wall"                # "wall" or "periodic"
+    bc: str = "wall"                # "wall", "periodic" or "neumann"
     reconstruction: str = "linear"  # "linear" or "none"
     sources: list | None = None     # explicit source-term objects (overrides the flags above)
     t0: float = 0.0
@@ -85,7 +85,8 @@ class Scenario:
 
     def grid(self) -> vf.CartesianGrid:
         return vf.CartesianGrid(self.nx, self.ny, gc=2,
-                                boundary=vf.PeriodicBC() if self.bc == "periodic" else vf.WallBC(),
+                                boundary={"periodic": vf.PeriodicBC(), "neumann": vf.NeumannBC()}.get(self.bc,
+                                                                                                      vf.WallBC()),
                                 extent=[list(self.extent[0]), list(self.extent[1])])
 
     def source_terms(self) -> list:
