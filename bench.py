@@ -102,11 +102,14 @@ def profile_table(tag: str):
 
 
 def kernel_names(dtype: str) -> dict:
-    """Kernels the library runs for this precision (tiles for Float64, marching for Float32, VF_KERNELS overrides)."""
+    """Kernels the library runs for this precision (TMA-staged tiles for Float64,
+    marching for Float32; VF_KERNELS and VF_TMA=0 override)."""
     variant = os.environ.get("VF_KERNELS", "tile" if dtype == "f64" else "march")
     t = "double" if dtype == "f64" else "float"
     if variant == "march":
         return {"flux": f"k_flux_march<{t},64>", "stage": f"k_stage_march<{t},64>"}
+    if dtype == "f64" and os.environ.get("VF_TMA", "1") != "0":
+        return {"flux": "k_flux_tma<double>", "stage": "k_stage2_tma<double>"}
     return {"flux": f"k_flux<{t}>", "stage": f"k_stage2<{t}>"}
 
 
@@ -200,13 +203,16 @@ def oracle_sim(sc, real_bytes=8):
     return o
 
 
-def cpu_rate(sc, warmup: int, steps: int | None, budget_s: float = 12.0, max_steps: int = 30):
-    """Oracle (the restated reference CPU path) on all host threads: cell-updates/s.
+def cpu_rate(sc, warmup: int, steps: int | None, budget_s: float = 12.0, max_steps: int = 30,
+             threads: int | None = None, o=None):
+    """Oracle (the restated reference CPU path) on all host threads (or the
+    given number): cell-updates/s.
 
-    With steps=None the number of steps is chosen to fit budget_s (at most max_steps)."""
+    With steps=None the number of steps is chosen to fit budget_s (at most
+    max_steps, at least one). `o` continues an existing oracle simulator."""
     from oracle import vf_oracle as O
-    threads = O.set_threads(os.cpu_count() or 1)
-    o = oracle_sim(sc)
+    threads = O.set_threads(threads or os.cpu_count() or 1)
+    o = o if o is not None else oracle_sim(sc)
     for _ in range(warmup):
         o.perform_step(math.inf)
     if steps is None:
@@ -691,10 +697,14 @@ def main():
         sim.close()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, threads, steps, el = cpu_rate(sc, 0, None)
+        o = oracle_sim(sc)
+        v, threads, steps, el = cpu_rate(sc, 0, None, o=o)
+        v1, _, steps1, el1 = cpu_rate(sc, 0, None, budget_s=6.0, threads=1, o=o)
         cpu = {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
                "sample": f"{steps} RK2 steps of the {sc.nx}x{sc.ny} Float64 workload from its initial state "
-                         f"({el:.1f} s, OpenMP over rows)"}
+                         f"({el:.1f} s, OpenMP over rows)",
+               "single_core": {"value": v1, "unit": METRIC, "cores": 1,
+                               "sample": f"the next {steps1} RK2 step(s) on one thread ({el1:.1f} s)"}}
     ens = serving = None
     if rank == 0 and world == 1 and not args.no_ensemble:
         ens = measure_ensemble(args, local)

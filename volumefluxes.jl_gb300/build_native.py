@@ -3,7 +3,8 @@
 Seven translation units compile in parallel with nvcc and link into one shared
 library with the CUDA runtime linked statically:
 
-  vf_f64.cu  Float64 kernels, -fmad=false (each operation rounds as in Julia)
+  vf_f64.cu  Float64 kernels, -fmad=false (each operation rounds as in Julia);
+             tile kernels held to 80 registers (three resident blocks per SM)
   vf_f32.cu  Float32 kernels, contraction and fast division allowed
   vf_abi.cu  the extern "C" boundary of include/volumefluxes_sm103.h
   vf_noalloc.cu  the allocation-free water-volume entry point
@@ -32,7 +33,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-strict-aliasing",
           f"-I{INCLUDE}", f"-I{CSRC}"]
 UNITS = {
-    "vf_f64.cu": ["-fmad=false"],
+    "vf_f64.cu": ["-fmad=false", "-DVF_TILE_MIN_BLOCKS=3"],
     "vf_f32.cu": ["-fmad=true", "-ftz=true", "-prec-sqrt=false"],
     "vf_abi.cu": [],
     "vf_noalloc.cu": [],

@@ -4,7 +4,9 @@
 // reference's dense Volume layout and the padded device layout, and drives the
 // step kernels (vf_launch.cuh). No CPU fallback exists: every compute entry
 // point runs on the GPU or returns an error.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <cmath>
 #include <cstdio>
@@ -168,6 +170,61 @@ void fill_phys(const vf_handle* h, vf::Phys<T>& p) {
       p.any_dynamic = 1;
     }
   }
+}
+
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+// (no link-time dependency on libcuda).
+PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+
+// Tiled tensor map of a Float64 array of `planes` planes (planes > 1: 3D) with
+// rows of `pitch` elements, plane stride `ps`, extent (nx, ny) elements; the
+// box is (bx, by[, planes]). Out-of-range elements read as zero.
+bool encode_f64(CUtensorMap* m, const void* base, long long nx, long long ny, long long pitch, long long ps,
+                int planes, int bx, int by) {
+  auto fn = encode_tiled();
+  if (!fn || !base) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)planes};
+  const cuuint64_t strides[2] = {(cuuint64_t)(pitch * 8), (cuuint64_t)(ps * 8)};
+  const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)planes};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const cuuint32_t rank = planes > 1 ? 3 : 2;
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, rank, const_cast<void*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Tensor maps of a Float64 handle's state, derivative, friction and corner
+// buffers for the TMA tile kernels (VF_TMA=0 turns them off). On any failure
+// the maps stay unused and the plain tile kernels run.
+void make_tma_maps(vf_handle* h) {
+  vf::TmaMaps& t = h->ad.tma;
+  std::memset(&t, 0, sizeof(t));
+  if (h->elem != 8) return;
+  if (const char* e = std::getenv("VF_TMA"))
+    if (std::strcmp(e, "0") == 0) return;
+  const long long nxp = vf::XOFF + h->N1;  // columns 0..XOFF-1 are padding
+  bool ok = true;
+  for (int k = 0; k < 2; ++k) {
+    ok = ok && encode_f64(&t.U[k], h->U[k], nxp, h->N2, h->P, h->PS, 3, vf::HX, vf::HY);
+    t.Ub[k] = h->U[k];
+  }
+  ok = ok && encode_f64(&t.L, h->L, nxp, h->N2, h->P, h->PS, 3, vf::HX, vf::HY);
+  t.Lb = h->L;
+  if (h->S) ok = ok && encode_f64(&t.S, h->S, nxp, h->N2, h->P, h->PS, 1, vf::HX, vf::HY);
+  t.Sb = h->S;
+  if (h->B) ok = ok && encode_f64(&t.B, h->B, nxp + 1, h->N2 + 1, h->PB, 0, 1, vf::BHX, vf::BHY);
+  t.Bb = h->B;
+  t.ok = ok ? 1 : 0;
 }
 
 // Column marching covers wall BCs, linear reconstruction and constant sources;
@@ -465,6 +522,7 @@ int vf_create(const vf_config* cfg, vf_handle** out) {
   h->af.L = static_cast<float*>(h->L);
   h->af.S = static_cast<float*>(h->S);
   h->af.rec = h->rec;
+  make_tma_maps(h);
   *out = h;
   return VF_OK;
 }

@@ -17,8 +17,12 @@
 //
 // Tiles are TX x TY interior cells; each block stages its tile with a 2-cell
 // halo of (w, hu, hv) and a 2..3-cell halo of bottom corners in shared memory.
+// The Float64 kernels of the per-step path (k_flux_tma, k_stage2_tma) stage
+// them with TMA copies (vf_tma.cuh); the ensemble and Float32 tiles load them
+// with plain loads.
 #pragma once
 #include "vf_math.cuh"
+#include "vf_tma.cuh"
 
 namespace vf {
 
@@ -28,7 +32,7 @@ constexpr int NT = 256;
 constexpr int CPT = TX * TY / NT;  // cells per thread
 constexpr int HX = TX + 4;
 constexpr int HY = TY + 4;
-constexpr int BHX = TX + 5;
+constexpr int BHX = TX + 6;  // TX + 5 corner columns are read; one more keeps Float64 rows 16-byte multiples
 constexpr int BHY = TY + 5;
 constexpr int LRN = (TX + 2) * TY > TX * (TY + 2) ? (TX + 2) * TY : TX * (TY + 2);
 constexpr int FN = (TX + 1) * TY > TX * (TY + 1) ? (TX + 1) * TY : TX * (TY + 1);
@@ -53,6 +57,7 @@ struct StepRecord {
   double explicit_max_dt;
   int explicit_mode;
   int force_dt;        // 1: every step uses forced_dt (a frozen dt sequence)
+  int wait_fault;      // set when a bounded wait for a tile copy gave up
   double forced_dt;
 };
 
@@ -292,6 +297,7 @@ __device__ __forceinline__ double speed_from_key<float>(unsigned long long k) {
 
 // ---------------------------------------------------------------------------
 // Flux pass: L(U0), S(U0) and the CFL maxima.
+// U and B come first: for Float64 both start 128-byte aligned (TMA destinations).
 template <typename T>
 struct SmemFlux {
   T U[3 * HX * HY];
@@ -301,26 +307,31 @@ struct SmemFlux {
   T F[3 * FN];
   unsigned long long red[2][NT / 32];
   T scal[8];
+  unsigned long long bar;  // mbarrier of the tile copies
+  int plain;               // 1: the tile was not staged by TMA, load it the plain way
 };
 
 // Flux pass over one tile at (x0, y0) (block-collective): L(U0) and S(U0) to
 // global memory; mx, my accumulate this thread's share of the CFL maxima.
 // t is the step's start time (time-dependent sources).
-template <typename T, bool CG>
+// STAGED: s.U and s.B already hold the tile (TMA).
+template <typename T, bool CG, bool STAGED = false>
 __device__ __forceinline__ void flux_tile(const Geom<T>& g, const Phys<T>& p, const T* U, const T* __restrict__ B,
                                           T* Lout, T* Sout, int x0, int y0, SmemFlux<T>& s, double t, T& mx, T& my) {
   const int tid = threadIdx.x;
   const int nvx = min(TX, g.gc + g.nx - x0), nvy = min(TY, g.gc + g.ny - y0);
 
-  for (int idx = tid; idx < HX * HY; idx += NT) {
-    const int lx = idx % HX, ly = idx / HX;
-    const int gx = x0 - 2 + lx, gy = y0 - 2 + ly;
-    const bool ok = gx < g.N1 && gy < g.N2;
-    const long long o = sidx(g, gx, gy);
+  if constexpr (!STAGED) {
+    for (int idx = tid; idx < HX * HY; idx += NT) {
+      const int lx = idx % HX, ly = idx / HX;
+      const int gx = x0 - 2 + lx, gy = y0 - 2 + ly;
+      const bool ok = gx < g.N1 && gy < g.N2;
+      const long long o = sidx(g, gx, gy);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) s.U[k * HX * HY + idx] = ok ? gld<CG>(U + k * g.PS + o) : (T)0;
+      for (int k = 0; k < 3; ++k) s.U[k * HX * HY + idx] = ok ? gld<CG>(U + k * g.PS + o) : (T)0;
+    }
+    if (!g.bottom_const) load_corners(g, B, s.B, x0, y0);
   }
-  if (!g.bottom_const) load_corners(g, B, s.B, x0, y0);
   if (p.any_dynamic && tid == 0) point_scalars<T>(p, t, s.scal);
   __syncthreads();
 
@@ -390,6 +401,57 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_flux(Geom<T> g, Phys
   flux_tile<T, false>(g, p, U, B, Lout, Sout, x0, y0, s, t, mx, my);
 
   // CFL maxima: warp shuffle, then one atomic per block and direction.
+  unsigned long long kx = 0, ky = 0;
+  block_speed_keys<T>(mx, my, s.red, kx, ky);
+  if (threadIdx.x == 0) {
+    atomicMax(&rec->speed_bits[parity][0], kx);
+    atomicMax(&rec->speed_bits[parity][1], ky);
+  }
+}
+
+// Bytes of one staged tile of n planes, and of the corner tile.
+template <typename T>
+__host__ __device__ constexpr unsigned tile_bytes(int planes) { return (unsigned)(planes * HX * HY * sizeof(T)); }
+template <typename T>
+__host__ __device__ constexpr unsigned corner_bytes() { return (unsigned)(BHX * BHY * sizeof(T)); }
+
+// k_flux with the tile staged by TMA (Float64). Thread 0 issues one 3D copy of
+// the three state planes and one 2D copy of the corners; everyone waits on the
+// mbarrier, then the flux pass runs as in k_flux.
+template <typename T>
+__global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS)
+    k_flux_tma(Geom<T> g, Phys<T> p, const __grid_constant__ CUtensorMap mU, const __grid_constant__ CUtensorMap mB,
+               const T* __restrict__ U, const T* __restrict__ B, T* __restrict__ Lout, T* __restrict__ Sout,
+               StepRecord* rec, int parity) {
+  static_assert(sizeof(T) == 8, "TMA tiles are Float64 (the tile origin is 16-byte aligned only for 8-byte cells)");
+  if (!rec->active[parity]) return;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  SmemFlux<T>& s = *reinterpret_cast<SmemFlux<T>*>(smem_raw);
+  const int x0 = g.gc + blockIdx.x * TX, y0 = g.gc + blockIdx.y * TY;
+  const int cx = x0 - 2 + XOFF, cy = y0 - 2;
+  if (threadIdx.x == 0) {
+    const bool ok = tma_ok(cx, (int)sizeof(T), s.U) && (g.bottom_const || tma_ok(cx, (int)sizeof(T), s.B));
+    s.plain = ok ? 0 : 1;
+    if (ok) {
+      mbar_init(&s.bar, 1);
+      mbar_expect_tx(&s.bar, tile_bytes<T>(3) + (g.bottom_const ? 0u : corner_bytes<T>()));
+      tma_load_3d(s.U, &mU, cx, cy, 0, &s.bar);
+      if (!g.bottom_const) tma_load_2d(s.B, &mB, cx, cy, &s.bar);
+    }
+  }
+  __syncthreads();
+  if (!s.plain && !mbar_wait_bounded(&s.bar, 0)) {
+    rec->wait_fault = 1;
+    s.plain = 1;  // every thread that gives up sets it; the barrier below makes it uniform
+  }
+  __syncthreads();
+  const double t = p.any_dynamic ? rec->t[parity] : 0.0;
+  T mx = (T)0, my = (T)0;
+  if (s.plain)
+    flux_tile<T, false, false>(g, p, U, B, Lout, Sout, x0, y0, s, t, mx, my);
+  else
+    flux_tile<T, false, true>(g, p, U, B, Lout, Sout, x0, y0, s, t, mx, my);
+
   unsigned long long kx = 0, ky = 0;
   block_speed_keys<T>(mx, my, s.red, kx, ky);
   if (threadIdx.x == 0) {
@@ -572,29 +634,40 @@ __device__ __forceinline__ void neumann_outer(const Geom<T>& g, const Phys<T>& p
 
 // ---------------------------------------------------------------------------
 // RK2 stage pass.
+// L, R and F come first and are contiguous: before the stage-2 derivative
+// overwrites them they hold the TMA-staged halo tiles of U0 (3 planes), L (3)
+// and S (1), STAGE_PLANES planes of HX x HY from offset 0 (k_stage2_tma).
+// For Float64 every TMA destination starts 128-byte aligned.
 template <typename T>
 struct SmemStage {
-  T U1[3 * HX * HY];
-  T U0[3 * TX * TY];
-  T B[BHX * BHY];
   T L[3 * LRN];
   T R[3 * LRN];
   T F[3 * FN];
+  T U1[3 * HX * HY];
+  T U0[3 * TX * TY];
+  T B[BHX * BHY];
   double dt;
   T scal[8];
+  unsigned long long bar;  // mbarrier of the tile copies
+  int plain;               // 1: the tile was not staged by TMA
 };
+constexpr int STAGE_PLANES = 7;
+static_assert(3 * LRN + 3 * LRN + 3 * FN >= STAGE_PLANES * HX * HY, "stage staging area must fit in L, R, F");
 
 // RK2 stage pass over one tile at (x0, y0) (block-collective): U2 with its
 // ghosts into Uo. dt is the step's dt, t its start time.
-template <typename T, bool CG>
+// STAGED: the halo tiles of U0, L, S sit at the start of s (planes of HX x HY:
+// U0 0..2, L 3..5, S 6) and s.B holds the corners (TMA).
+template <typename T, bool CG, bool STAGED = false>
 __device__ __forceinline__ void stage2_tile(const Geom<T>& g, const Phys<T>& p, const T* U0, const T* __restrict__ B,
                                             const T* Lin, const T* Sin, T* Uo, int x0, int y0, SmemStage<T>& s,
                                             double dt, double t) {
   const int tid = threadIdx.x;
   const int nvx = min(TX, g.gc + g.nx - x0), nvy = min(TY, g.gc + g.ny - y0);
   if (p.any_dynamic && tid == 1) point_scalars<T>(p, t, s.scal);
-  if (!g.bottom_const) load_corners(g, B, s.B, x0, y0);
+  if (!STAGED && !g.bottom_const) load_corners(g, B, s.B, x0, y0);
   __syncthreads();
+  const T* stg = s.L;  // staged planes (STAGED only)
   const T tdt = (T)dt;
   BTile<T> bt{s.B, g.bottom_const, g.bconst};
 
@@ -608,11 +681,27 @@ __device__ __forceinline__ void stage2_tile(const Geom<T>& g, const Phys<T>& p, 
     const bool yin = gy >= g.gc && gy < g.gc + g.ny;
     T w = (T)0, hu = (T)0, hv = (T)0;
     if (xin && yin) {
-      const long long o = sidx(g, gx, gy);
-      const T a0 = gld<CG>(U0 + o), a1 = gld<CG>(U0 + g.PS + o), a2 = gld<CG>(U0 + 2 * g.PS + o);
-      const T S = p.friction ? gld<CG>(Sin + o) : (T)0;
-      stage1_point<T>(p, tdt, a0, a1, a2, gld<CG>(Lin + o), gld<CG>(Lin + g.PS + o), gld<CG>(Lin + 2 * g.PS + o), S,
-                      bt.cell(lx, ly), w, hu, hv);
+      T a0, a1, a2, l0, l1, l2, S;
+      if constexpr (STAGED) {
+        constexpr int A = HX * HY;
+        a0 = stg[idx];
+        a1 = stg[A + idx];
+        a2 = stg[2 * A + idx];
+        l0 = stg[3 * A + idx];
+        l1 = stg[4 * A + idx];
+        l2 = stg[5 * A + idx];
+        S = p.friction ? stg[6 * A + idx] : (T)0;
+      } else {
+        const long long o = sidx(g, gx, gy);
+        a0 = gld<CG>(U0 + o);
+        a1 = gld<CG>(U0 + g.PS + o);
+        a2 = gld<CG>(U0 + 2 * g.PS + o);
+        l0 = gld<CG>(Lin + o);
+        l1 = gld<CG>(Lin + g.PS + o);
+        l2 = gld<CG>(Lin + 2 * g.PS + o);
+        S = p.friction ? gld<CG>(Sin + o) : (T)0;
+      }
+      stage1_point<T>(p, tdt, a0, a1, a2, l0, l1, l2, S, bt.cell(lx, ly), w, hu, hv);
       if (lx >= 0 && lx < TX && ly >= 0 && ly < TY) {
         const int t = ly * TX + lx;
         s.U0[t] = a0;
@@ -688,6 +777,55 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS) k_stage2(Geom<T> g, Ph
   __syncthreads();
   const double dt = s.dt;
   stage2_tile<T, false>(g, p, U0, B, Lin, Sin, Uo, x0, y0, s, dt, rec->t[parity]);
+  if (root) advance_record<T>(rec, parity, dt);
+}
+
+// k_stage2 with the halo tiles of U0, L, S and the corners staged by TMA
+// (Float64): three or four copies on one mbarrier, issued by thread 0.
+template <typename T>
+__global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS)
+    k_stage2_tma(Geom<T> g, Phys<T> p, const __grid_constant__ CUtensorMap mU, const __grid_constant__ CUtensorMap mL,
+                 const __grid_constant__ CUtensorMap mS, const __grid_constant__ CUtensorMap mB,
+                 const T* __restrict__ U0, const T* __restrict__ B, const T* __restrict__ Lin,
+                 const T* __restrict__ Sin, T* __restrict__ Uo, StepRecord* rec, int parity) {
+  static_assert(sizeof(T) == 8, "TMA tiles are Float64 (the tile origin is 16-byte aligned only for 8-byte cells)");
+  const bool root = blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0;
+  if (!rec->active[parity]) {
+    if (root) carry_record(rec, parity);
+    return;
+  }
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  SmemStage<T>& s = *reinterpret_cast<SmemStage<T>*>(smem_raw);
+  const int x0 = g.gc + blockIdx.x * TX, y0 = g.gc + blockIdx.y * TY;
+  const int cx = x0 - 2 + XOFF, cy = y0 - 2;
+  if (threadIdx.x == 0) {
+    constexpr int A = HX * HY;
+    T* stg = s.L;
+    const bool ok = tma_ok(cx, (int)sizeof(T), stg) && tma_ok(cx, (int)sizeof(T), stg + 3 * A) &&
+                    tma_ok(cx, (int)sizeof(T), stg + 6 * A) && (g.bottom_const || tma_ok(cx, (int)sizeof(T), s.B));
+    s.plain = ok ? 0 : 1;
+    if (ok) {
+      mbar_init(&s.bar, 1);
+      mbar_expect_tx(&s.bar, tile_bytes<T>(6) + (p.friction ? tile_bytes<T>(1) : 0u) +
+                                 (g.bottom_const ? 0u : corner_bytes<T>()));
+      tma_load_3d(stg, &mU, cx, cy, 0, &s.bar);
+      tma_load_3d(stg + 3 * A, &mL, cx, cy, 0, &s.bar);
+      if (p.friction) tma_load_2d(stg + 6 * A, &mS, cx, cy, &s.bar);
+      if (!g.bottom_const) tma_load_2d(s.B, &mB, cx, cy, &s.bar);
+    }
+    s.dt = step_dt<T>(g, rec, parity);
+  }
+  __syncthreads();
+  if (!s.plain && !mbar_wait_bounded(&s.bar, 0)) {
+    rec->wait_fault = 1;
+    s.plain = 1;
+  }
+  __syncthreads();
+  const double dt = s.dt;
+  if (s.plain)
+    stage2_tile<T, false, false>(g, p, U0, B, Lin, Sin, Uo, x0, y0, s, dt, rec->t[parity]);
+  else
+    stage2_tile<T, false, true>(g, p, U0, B, Lin, Sin, Uo, x0, y0, s, dt, rec->t[parity]);
   if (root) advance_record<T>(rec, parity, dt);
 }
 

@@ -18,6 +18,7 @@ struct StepArgs {
   T* L;
   T* S;
   StepRecord* rec;
+  TmaMaps tma;  // Float64 tile kernels: TMA staging when tma.ok and the buffers match
 };
 
 // One full step reading Uin, writing Uout; parity selects the record slot.

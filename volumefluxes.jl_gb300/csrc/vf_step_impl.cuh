@@ -26,6 +26,12 @@ cudaError_t configure_impl() {
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_stage2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemStage<T>));
   if (e != cudaSuccess) return e;
+  if constexpr (sizeof(T) == 8) {
+    e = cudaFuncSetAttribute(k_flux_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemFlux<T>));
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_stage2_tma<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemStage<T>));
+    if (e != cudaSuccess) return e;
+  }
   e = cudaFuncSetAttribute(k_ensemble<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemEns<T>));
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_ensemble<T, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -93,8 +99,31 @@ dim3 march_grid(const Geom<T>& g) {
   return dim3((nstrips + MWPB - 1) / MWPB, (g.ny + MarchSeg<T>::value - 1) / MarchSeg<T>::value);
 }
 
+// Index of the handle volume Uin is (0 or 1) when the launch can stage its
+// tiles with the handle's tensor maps, else -1.
+template <typename T>
+int tma_volume(const StepArgs<T>& a, const T* Uin) {
+  if constexpr (sizeof(T) != 8) {
+    return -1;
+  } else {
+    if (!a.tma.ok || a.variant != 1 || a.L != a.tma.Lb || a.S != a.tma.Sb || a.B != a.tma.Bb) return -1;
+    if (Uin == a.tma.Ub[0]) return 0;
+    if (Uin == a.tma.Ub[1]) return 1;
+    return -1;
+  }
+}
+
 template <typename T>
 cudaError_t launch_flux_impl(const StepArgs<T>& a, const T* Uin, int parity, cudaStream_t st) {
+  if constexpr (sizeof(T) == 8) {
+    const int v = tma_volume<T>(a, Uin);
+    if (v >= 0) {
+      const dim3 grid((a.g.nx + TX - 1) / TX, (a.g.ny + TY - 1) / TY);
+      k_flux_tma<T><<<grid, NT, sizeof(SmemFlux<T>), st>>>(a.g, a.p, a.tma.U[v], a.tma.B, Uin, a.B, a.L, a.S, a.rec,
+                                                            parity);
+      return cudaGetLastError();
+    }
+  }
   if (a.variant == 0) {
     k_flux_march<T, MarchSeg<T>::value><<<march_grid(a.g), MW * MWPB, 0, st>>>(a.g, a.p, Uin, a.B, a.L, a.S, a.rec,
                                                                                 parity);
@@ -112,6 +141,14 @@ cudaError_t launch_stage_impl(const StepArgs<T>& a, const T* Uin, T* Uout, int p
     k_stage_march<T, MarchSeg<T>::value><<<march_grid(a.g), MW * MWPB, 0, st>>>(a.g, a.p, Uin, a.B, a.L, a.S, Uout,
                                                                                  a.rec, parity);
   } else if (a.rk2) {
+    if constexpr (sizeof(T) == 8) {
+      const int v = tma_volume<T>(a, Uin);
+      if (v >= 0) {
+        k_stage2_tma<T><<<grid, NT, sizeof(SmemStage<T>), st>>>(a.g, a.p, a.tma.U[v], a.tma.L, a.tma.S, a.tma.B, Uin,
+                                                                 a.B, a.L, a.S, Uout, a.rec, parity);
+        return cudaGetLastError();
+      }
+    }
     k_stage2<T><<<grid, NT, sizeof(SmemStage<T>), st>>>(a.g, a.p, Uin, a.B, a.L, a.S, Uout, a.rec, parity);
   } else {
     k_apply_fe<T><<<grid, NT, 0, st>>>(a.g, a.p, Uin, a.B, a.L, a.S, Uout, a.rec, parity);
