@@ -29,12 +29,21 @@
 #endif
 // Float64 quotients sharing a divisor through one refined reciprocal and an
 // exact rounding test (1), or one IEEE division each (0); both are exact.
-// Measured on the 4096^2 wet/dry step the shared form was slower (41.6 vs
-// 31.5 ms/step): the hardware division costs about seven FP64 operations, and
-// the rounding test plus its 64-bit integer work outweigh the saved Newton
-// steps, so one division each is the default.
+// Measured on GB300 the shared form is slower: 32 G quotients/s against 56-59
+// for the hardware division in a throughput test (four quotients per divisor,
+// every one on the fast path, bitwise equal), and 41.1 vs 31.0 ms per 4096^2
+// wet/dry step, so one division each is the default.
 #ifndef VF_FP64_SHARED_DIV
 #define VF_FP64_SHARED_DIV 0
+#endif
+// Float32 reciprocals and cube roots from the special-function unit (1:
+// rcp.approx, and cbrt(x) = 2^(log2|x| / 3) with the sign of x; a few ulps) or
+// the correctly rounded reciprocal and the libm cube root (0). Float32 results
+// are stated against the Float64 oracle, not claimed bitwise. Measured on the
+// 4096^2 wet/dry step (Float32 is instruction-issue bound): 0.919 ms with the
+// special-function unit, 1.069 ms without.
+#ifndef VF_F32_FAST_SFU
+#define VF_F32_FAST_SFU 1
 #endif
 
 namespace vf {
@@ -120,13 +129,17 @@ struct Arith<float> {
   static __device__ __forceinline__ float max(float x, float y) { return fmaxf(x, y); }
   static __device__ __forceinline__ float min(float x, float y) { return fminf(x, y); }
   static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+#if VF_F32_FAST_SFU
+  static __device__ __forceinline__ float rcp(float b) { return __fdividef(1.0f, b); }
+#else
   static __device__ __forceinline__ float rcp(float b) { return __frcp_rn(b); }
+#endif
   static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
   // Quotients over one divisor: one reciprocal, then products.
   struct Recip {
     float r;
   };
-  static __device__ __forceinline__ Recip recip(float b) { return Recip{__frcp_rn(b)}; }
+  static __device__ __forceinline__ Recip recip(float b) { return Recip{rcp(b)}; }
   static __device__ __forceinline__ float div_by(const Recip& R, float a) { return a * R.r; }
 };
 
@@ -198,7 +211,15 @@ static __device__ __noinline__ double cr_cbrt(double x) {
 
 template <typename T> __device__ __forceinline__ T vcbrt(T x);
 template <> __device__ __forceinline__ double vcbrt<double>(double x) { return cr_cbrt(x); }
+#if VF_F32_FAST_SFU
+template <> __device__ __forceinline__ float vcbrt<float>(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(__log2f(fabsf(x)) * (1.0f / 3.0f)));
+  return copysignf(y, x);
+}
+#else
 template <> __device__ __forceinline__ float vcbrt<float>(float x) { return cbrtf(x); }
+#endif
 
 // Back-compat names used by the tile kernels.
 template <typename T> __device__ __forceinline__ T jmax(T x, T y) { return Arith<T>::max(x, y); }
