@@ -216,6 +216,9 @@ void make_tma_maps(vf_handle* h) {
   bool ok = true;
   for (int k = 0; k < 2; ++k) {
     ok = ok && encode_f64(&t.U[k], h->U[k], nxp, h->N2, h->P, h->PS, 3, vf::HX, vf::HY);
+    // tile stores: extent ends at the last interior row and at or before the last interior column
+    ok = ok && encode_f64(&t.Ust[k], h->U[k], vf::tma_store_cols(vf::XOFF + h->cfg.gc + h->cfg.nx),
+                          h->cfg.gc + h->cfg.ny, h->P, h->PS, 3, vf::TX, vf::TY);
     t.Ub[k] = h->U[k];
   }
   ok = ok && encode_f64(&t.L, h->L, nxp, h->N2, h->P, h->PS, 3, vf::HX, vf::HY);

@@ -516,13 +516,16 @@ __device__ __forceinline__ void carry_record(StepRecord* rec, int parity) {
 // Ghosts written by the owner of each boundary source cell: wall mirrors
 // (src/bc.jl:81-110; x ghosts negate hu, y ghosts hv) or periodic copies
 // (src/bc.jl:29-40). Corner ghosts are never written, as in the reference.
-template <typename T>
+// INTERIOR = false: the ghost copies only (the cell itself is stored elsewhere).
+template <typename T, bool INTERIOR = true>
 __device__ __forceinline__ void store_with_ghosts(const Geom<T>& g, T* __restrict__ Uo, int gx, int gy, T w, T hu,
                                                   T hv) {
-  const long long o = sidx(g, gx, gy);
-  Uo[o] = w;
-  Uo[g.PS + o] = hu;
-  Uo[2 * g.PS + o] = hv;
+  if constexpr (INTERIOR) {
+    const long long o = sidx(g, gx, gy);
+    Uo[o] = w;
+    Uo[g.PS + o] = hu;
+    Uo[2 * g.PS + o] = hv;
+  }
   int gxs[2] = {-1, -1}, gys[2] = {-1, -1};
   const T sx = g.bc == 1 ? (T)-1 : (T)1;  // normal momentum sign across a ghost
   if (g.bc == 2) {
@@ -657,7 +660,9 @@ static_assert(3 * LRN + 3 * LRN + 3 * FN >= STAGE_PLANES * HX * HY, "stage stagi
 // RK2 stage pass over one tile at (x0, y0) (block-collective): U2 with its
 // ghosts into Uo. dt is the step's dt, t its start time.
 // STAGED: the halo tiles of U0, L, S sit at the start of s (planes of HX x HY:
-// U0 0..2, L 3..5, S 6) and s.B holds the corners (TMA).
+// U0 0..2, L 3..5, S 6) and s.B holds the corners (TMA); the interior of U2
+// goes to s.U0 (in place: each thread overwrites the cells it read) for a
+// tensor store by the caller, its ghost copies straight to Uo.
 template <typename T, bool CG, bool STAGED = false>
 __device__ __forceinline__ void stage2_tile(const Geom<T>& g, const Phys<T>& p, const T* U0, const T* __restrict__ B,
                                             const T* Lin, const T* Sin, T* Uo, int x0, int y0, SmemStage<T>& s,
@@ -753,7 +758,14 @@ __device__ __forceinline__ void stage2_tile(const Geom<T>& g, const Phys<T>& p, 
     const T Bc = bt.cell(lx, ly);
     if (p.friction && friction_active<T>(v1, v2)) apply_friction<T>(tdt, friction_factor<T>(p, v0, v1, v2, Bc), hu, hv);
     dry_clamp<T>(p, w, hu, hv, Bc);
-    store_with_ghosts<T>(g, Uo, x0 + lx, y0 + ly, w, hu, hv);
+    if (STAGED && x0 + lx + XOFF < tma_store_cols(XOFF + g.gc + g.nx)) {
+      s.U0[c] = w;  // stored by the tile's tensor store
+      s.U0[TX * TY + c] = hu;
+      s.U0[2 * TX * TY + c] = hv;
+      store_with_ghosts<T, false>(g, Uo, x0 + lx, y0 + ly, w, hu, hv);
+    } else {
+      store_with_ghosts<T>(g, Uo, x0 + lx, y0 + ly, w, hu, hv);
+    }
     if (g.bc == 3) {
       if (x0 + lx == g.gc + g.nx - 1) neumann_outer<T, CG>(g, p, tdt, U0, B, s.scal, g.N1 - 1, y0 + ly, 0, true, Uo);
       if (y0 + ly == g.gc + g.ny - 1) neumann_outer<T, CG>(g, p, tdt, U0, B, s.scal, x0 + lx, g.N2 - 1, 1, true, Uo);
@@ -786,6 +798,7 @@ template <typename T>
 __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS)
     k_stage2_tma(Geom<T> g, Phys<T> p, const __grid_constant__ CUtensorMap mU, const __grid_constant__ CUtensorMap mL,
                  const __grid_constant__ CUtensorMap mS, const __grid_constant__ CUtensorMap mB,
+                 const __grid_constant__ CUtensorMap mUo,
                  const T* __restrict__ U0, const T* __restrict__ B, const T* __restrict__ Lin,
                  const T* __restrict__ Sin, T* __restrict__ Uo, StepRecord* rec, int parity) {
   static_assert(sizeof(T) == 8, "TMA tiles are Float64 (the tile origin is 16-byte aligned only for 8-byte cells)");
@@ -802,7 +815,8 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS)
     constexpr int A = HX * HY;
     T* stg = s.L;
     const bool ok = tma_ok(cx, (int)sizeof(T), stg) && tma_ok(cx, (int)sizeof(T), stg + 3 * A) &&
-                    tma_ok(cx, (int)sizeof(T), stg + 6 * A) && (g.bottom_const || tma_ok(cx, (int)sizeof(T), s.B));
+                    tma_ok(cx, (int)sizeof(T), stg + 6 * A) && (g.bottom_const || tma_ok(cx, (int)sizeof(T), s.B)) &&
+                    tma_ok(x0 + XOFF, (int)sizeof(T), s.U0);
     s.plain = ok ? 0 : 1;
     if (ok) {
       mbar_init(&s.bar, 1);
@@ -822,10 +836,19 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS)
   }
   __syncthreads();
   const double dt = s.dt;
-  if (s.plain)
+  if (s.plain) {
     stage2_tile<T, false, false>(g, p, U0, B, Lin, Sin, Uo, x0, y0, s, dt, rec->t[parity]);
-  else
+  } else {
     stage2_tile<T, false, true>(g, p, U0, B, Lin, Sin, Uo, x0, y0, s, dt, rec->t[parity]);
+    // The interior tile from s.U0 (128-byte aligned, x0 + XOFF even) in one tensor store.
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_store_3d(&mUo, s.U0, x0 + XOFF, y0, 0);
+      bulk_commit();
+      bulk_wait_all();
+    }
+  }
   if (root) advance_record<T>(rec, parity, dt);
 }
 

@@ -143,9 +143,10 @@ cudaError_t launch_stage_impl(const StepArgs<T>& a, const T* Uin, T* Uout, int p
   } else if (a.rk2) {
     if constexpr (sizeof(T) == 8) {
       const int v = tma_volume<T>(a, Uin);
-      if (v >= 0) {
-        k_stage2_tma<T><<<grid, NT, sizeof(SmemStage<T>), st>>>(a.g, a.p, a.tma.U[v], a.tma.L, a.tma.S, a.tma.B, Uin,
-                                                                 a.B, a.L, a.S, Uout, a.rec, parity);
+      if (v >= 0 && Uout == a.tma.Ub[v ^ 1]) {
+        k_stage2_tma<T><<<grid, NT, sizeof(SmemStage<T>), st>>>(a.g, a.p, a.tma.U[v], a.tma.L, a.tma.S, a.tma.B,
+                                                                 a.tma.Ust[v ^ 1], Uin, a.B, a.L, a.S, Uout, a.rec,
+                                                                 parity);
         return cudaGetLastError();
       }
     }

@@ -12,6 +12,15 @@
 // coordinate times the element size is a multiple of 16 bytes (the tiles start
 // at even columns of Float64 rows), and the shared-memory destination is
 // 128-byte aligned. A block that cannot use TMA loads its tile the plain way.
+// The stage pass also writes its output tile (the interior cells; ghost cells
+// are written with plain stores) from shared memory with one tensor store.
+// Out-of-range clipping of a store is not exact to the element along x: with
+// the extent ending inside a 16-byte chunk, the store also wrote the rest of
+// that chunk (the first ghost column of a grid with an odd interior width,
+// measured on GB300). So the store maps' x extent ends at a 32-byte multiple
+// at or below the last interior column (tma_store_cols), and the interior
+// columns past it are written with plain stores; no tensor store reaches a
+// ghost cell or padding.
 // Waits are bounded: a wait that gives up records the fact in the step record
 // and the block loads its tile the plain way.
 #pragma once
@@ -26,6 +35,7 @@ namespace vf {
 // uses them only when its buffers are the ones the maps were made for.
 struct TmaMaps {
   CUtensorMap U[2];  // the two state volumes: 3D (x, y, plane), box HX x HY x 3
+  CUtensorMap Ust[2];  // the same volumes for tile stores: interior extent only, box TX x TY x 3
   CUtensorMap L;     // stage-1 derivative planes, same shape
   CUtensorMap S;     // friction factor, 2D, box HX x HY
   CUtensorMap B;     // bottom corners, 2D, box BHX x BHY
@@ -35,6 +45,15 @@ struct TmaMaps {
   const void* Bb;
   int ok;
 };
+
+// x extent (in 8-byte elements, from the row start) of a tile-store map for
+// rows whose interior ends before column `cols`: rounded down to 32 bytes.
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+    inline int tma_store_cols(int cols) {
+  return cols & ~3;
+}
 
 #if defined(__CUDACC__)
 
@@ -89,6 +108,20 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
       : "memory");
 }
+
+// Shared -> global tile store (bulk group). Elements outside the map's extent
+// are not written. The source must be made visible to the async proxy first
+// (fence_async_smem by the writing threads, then a block barrier).
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, const void* src, int c0, int c1, int c2) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(smem_addr(src)), "r"(c0), "r"(c1), "r"(c2)
+               : "memory");
+}
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// Waits until this thread's committed bulk stores have completed.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // The copy rules this file relies on: x * element size a multiple of 16 bytes,
 // destination 128-byte aligned.
