@@ -163,7 +163,16 @@ __device__ __forceinline__ int cmp192(uint64_t a0, uint64_t a1, uint64_t a2, uin
   return 0;
 }
 
+// Out of line by default (the friction law calls it from two places per cell
+// and step); VF_CBRT_INLINE=1 inlines it.
+#ifndef VF_CBRT_INLINE
+#define VF_CBRT_INLINE 0
+#endif
+#if VF_CBRT_INLINE
+static __device__ __forceinline__ double cr_cbrt(double x) {
+#else
 static __device__ __noinline__ double cr_cbrt(double x) {
+#endif
   if (x == 0.0 || !isfinite(x)) return x;
   const bool neg = signbit(x);
   double a = fabs(x);
