@@ -335,6 +335,8 @@ int push_record(vf_handle* h) {
 int pull_record(vf_handle* h) {
   VF_CK(h, cudaMemcpyAsync(h->rec_h, h->rec, sizeof(vf::StepRecord), cudaMemcpyDeviceToHost, h->stream));
   VF_CK(h, cudaStreamSynchronize(h->stream));
+  if (h->rec_h->wait_fault)  // the block still loaded its tile the plain way, but the copy engine stalled for seconds
+    return fail(h, VF_ECUDA, "a bounded wait for a TMA tile copy gave up (the tile was then loaded with plain loads)");
   return VF_OK;
 }
 
