@@ -180,6 +180,13 @@ int vf_time_steps(vf_handle* h, int64_t n_steps, float* ms_out);
  * of the stage (RK2) or apply (forward Euler) passes. */
 int vf_time_kernels(vf_handle* h, int64_t n_steps, float* ms_flux, float* ms_stage);
 
+/* Self-test of the bounded wait the TMA tile kernels use for their tile
+ * copies (an mbarrier in shared memory): one warp waits on a barrier that is
+ * completed (arrive = 1) or never completed (arrive = 0) and gives up after
+ * `iterations` polls; *gave_up receives 1 when the wait ran out. The kernel
+ * returns either way. No reference counterpart (failure-detection test hook). */
+int vf_selftest_tile_wait(int32_t device, int32_t arrive, int32_t iterations, int32_t* gave_up);
+
 /* ---- Batched ensemble ------------------------------------------------------
  * Advances many independent simulations, each a handle set up as above, each
  * to its own end time with its own CFL dt: the loop of simulate_to_time

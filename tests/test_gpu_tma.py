@@ -61,3 +61,21 @@ def test_tma_matches_plain_loads(case):
     b = run(make(), steps, tma=False)
     for x, y, name in zip(a, b, ("dt", "w", "hu", "hv")):
         assert np.array_equal(x.view(np.uint64), y.view(np.uint64)), f"{case}: {name} differs"
+
+
+def test_bounded_tile_wait_gives_up_and_returns():
+    """The wait the TMA kernels use for their copies ends on its own when the
+    copy never completes (a barrier nothing completes), and succeeds at once
+    when it does; the kernel returns either way and the context stays usable."""
+    import ctypes as C
+    from volumefluxes_sm103 import _native as N
+    lib = N.load()
+    out = C.c_int32(-1)
+    N.check(lib, None, lib.vf_selftest_tile_wait(0, 0, 2000, C.byref(out)))
+    assert out.value == 1
+    N.check(lib, None, lib.vf_selftest_tile_wait(0, 1, 2000, C.byref(out)))
+    assert out.value == 0
+    sim = S.circular_dam_break(32).build(vf.SM103Backend(np.float64))  # the device still steps afterwards
+    vf.perform_step(sim, math.inf)
+    assert np.isfinite(vf.current_interior_state(sim).h).all()
+    sim.close()

@@ -453,6 +453,18 @@ size_t handle_device_bytes(const vf_config* c) {
 }
 }  // namespace vf
 
+namespace {
+// One warp waits on an mbarrier that thread 0 completes (arrive) or that
+// nothing completes; *gave_up = 1 when any thread's bounded wait ran out.
+__global__ void k_selftest_tile_wait(int arrive, int iterations, int* gave_up) {
+  __shared__ unsigned long long bar;
+  if (threadIdx.x == 0) vf::mbar_init(&bar, 1);
+  __syncthreads();
+  if (arrive && threadIdx.x == 0) vf::mbar_arrive(&bar);
+  if (!vf::mbar_wait_bounded(&bar, 0, iterations)) atomicOr(gave_up, 1);
+}
+}  // namespace
+
 extern "C" {
 
 int vf_create(const vf_config* cfg, vf_handle** out) {
@@ -717,6 +729,26 @@ int vf_simulate(vf_handle* h, double t0, double endtime, int32_t match_endtime, 
   if (t_out) *t_out = h->rec_h->t[k & 1];
   if (steps_out) *steps_out = done;
   if (last_dt_out) *last_dt_out = h->rec_h->last_dt;
+  return VF_OK;
+}
+
+int vf_selftest_tile_wait(int32_t device, int32_t arrive, int32_t iterations, int32_t* gave_up) {
+  if (!gave_up || iterations < 1 || iterations > (1 << 22))
+    return fail(nullptr, VF_EINVAL, "gave_up must be non-NULL and iterations in [1, 2^22]");
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+  int* d = nullptr;
+  if ((e = cudaMalloc(&d, sizeof(int))) != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
+  e = cudaMemset(d, 0, sizeof(int));
+  if (e == cudaSuccess) {
+    k_selftest_tile_wait<<<1, 32>>>(arrive ? 1 : 0, iterations, d);
+    e = cudaGetLastError();
+  }
+  int v = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&v, d, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "tile-wait self-test");
+  *gave_up = v;
   return VF_OK;
 }
 

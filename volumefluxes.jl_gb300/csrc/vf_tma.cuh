@@ -84,11 +84,15 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
 }
 
 // Bounded wait for the phase to complete (each try_wait may suspend the
-// thread for a short time); false when it gave up.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned phase) {
-  for (int i = 0; i < (1 << 22); ++i)
+// thread for a short, hardware-bounded time); false when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned phase, int limit = 1 << 22) {
+  for (int i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, phase)) return true;
   return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1,
