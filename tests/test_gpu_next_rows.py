@@ -54,6 +54,9 @@ CASES = {
     "hills_neumann_partial_tiles_fe": (lambda: hills_rect(37, 19, bc="neumann", stepper="fe"), 60),
     "time_rain_and_horton_neumann_rk2": (lambda: terrain_sources(45, 33, bc="neumann"), 80),
     "dam_break_neumann_rk2": (lambda: S.Scenario(**{**S.circular_dam_break(64).__dict__, "bc": "neumann"}), 60),
+    "no_reconstruction_neumann_fe": (lambda: hills_rect(41, 29, bc="neumann", reconstruction="none", stepper="fe"), 60),
+    "hills_periodic_bh2021_nonpow2": (lambda: hills_rect(45, 35, bc="periodic", friction_law="bh2021",
+                                                         extent=((0.0, 30.0), (0.0, 21.0))), 60),
 }
 
 

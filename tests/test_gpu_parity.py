@@ -64,6 +64,8 @@ CASES = {
     "dry_circle_64_rk2": (lambda: dry_circle(64), 80),
     "eq_params_rho_g_cutoff": (lambda: hills_rect(40, 40, eq={"rho": 1.5, "g": 3.7, "depth_cutoff": 1e-4,
                                                             "desingularizing_kappa": 1e-6}, theta=1.7), 60),
+    # cell sizes that are not powers of two: 1/Δ * (F_r - F_l) rounds and ΔB/Δ is a division
+    "hills_50x30_nonpow2_cells": (lambda: hills_rect(50, 30, extent=((0.0, 37.0), (0.0, 23.0))), 60),
 }
 
 
