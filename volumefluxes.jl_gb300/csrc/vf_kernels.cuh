@@ -308,7 +308,7 @@ struct SmemFlux {
   unsigned long long red[2][NT / 32];
   T scal[8];
   unsigned long long bar;  // mbarrier of the tile copies
-  int plain;               // 1: the tile was not staged by TMA, load it the plain way
+  int plain;               // 0: staged by TMA; 1: not staged (alignment); 2: the wait gave up
 };
 
 // Flux pass over one tile at (x0, y0) (block-collective): L(U0) and S(U0) to
@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS)
   __syncthreads();
   if (!s.plain && !mbar_wait_bounded(&s.bar, 0)) {
     rec->wait_fault = 1;
-    s.plain = 1;  // every thread that gives up sets it; the barrier below makes it uniform
+    s.plain = 2;  // gave up; every thread that gives up sets it, the barrier below makes it uniform
   }
   __syncthreads();
   const double t = p.any_dynamic ? rec->t[parity] : 0.0;
@@ -458,6 +458,9 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS)
     atomicMax(&rec->speed_bits[parity][0], kx);
     atomicMax(&rec->speed_bits[parity][1], ky);
   }
+  // After a give-up, wait once more (bounded) so a late copy does not land
+  // after the block has released its shared memory.
+  if (s.plain == 2 && threadIdx.x == 0) mbar_wait_bounded(&s.bar, 0);
 }
 
 // dt of stage 1 from the CFL maxima, src/simulator.jl:147-150.
@@ -652,7 +655,7 @@ struct SmemStage {
   double dt;
   T scal[8];
   unsigned long long bar;  // mbarrier of the tile copies
-  int plain;               // 1: the tile was not staged by TMA
+  int plain;               // 0: staged by TMA; 1: not staged (alignment); 2: the wait gave up
 };
 constexpr int STAGE_PLANES = 7;
 static_assert(3 * LRN + 3 * LRN + 3 * FN >= STAGE_PLANES * HX * HY, "stage staging area must fit in L, R, F");
@@ -832,7 +835,7 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS)
   __syncthreads();
   if (!s.plain && !mbar_wait_bounded(&s.bar, 0)) {
     rec->wait_fault = 1;
-    s.plain = 1;
+    s.plain = 2;  // gave up
   }
   __syncthreads();
   const double dt = s.dt;
@@ -850,6 +853,7 @@ __global__ void __launch_bounds__(NT, VF_TILE_MIN_BLOCKS)
     }
   }
   if (root) advance_record<T>(rec, parity, dt);
+  if (s.plain == 2 && threadIdx.x == 0) mbar_wait_bounded(&s.bar, 0);  // a late copy lands before exit
 }
 
 // ---------------------------------------------------------------------------
