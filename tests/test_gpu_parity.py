@@ -186,3 +186,24 @@ def test_float32_error_against_float64_oracle(case, tol):
     assert max_rel(g.h, w) <= tol
     scale = max(np.abs(hu).max(), np.abs(hv).max())
     assert np.abs(g.hu - hu).max() <= 50 * tol * scale and np.abs(g.hv - hv).max() <= 50 * tol * scale
+
+
+def test_time_order_of_the_steppers_gpu():
+    # test/test_timesteppers.jl:70-87 on the device: forward Euler first order,
+    # RK2 second order in time, with every step forced to the same dt
+    from test_oracle_kats import smooth_bump, time_order
+
+    def run(stepper, dt, T):
+        sc = smooth_bump()
+        sc.stepper = stepper
+        sim = sc.build(vf.SM103Backend(np.float64))
+        for _ in range(int(round(T / dt))):
+            vf.perform_step(sim, dt)
+            sim.t += sim.current_timestep
+        w = vf.current_interior_state(sim).h.copy()
+        sim.close()
+        return w
+
+    order = time_order(run)
+    assert order["rk2"] == pytest.approx(2.0, abs=0.05)
+    assert order["fe"] == pytest.approx(1.0, abs=0.1)

@@ -259,3 +259,44 @@ def test_mass_conserved_without_sources():
     for _ in range(50):
         o.perform_step(math.inf)
     assert abs(o.interior()[0].sum() - w0) <= 1e-10 * w0
+
+
+def smooth_bump(n=64):
+    """A smooth wet bump on a flat bottom (no limiter switching near the crest
+    matters at this amplitude): the time-order test's initial state."""
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    h0 = 1.0 + 0.1 * np.exp(-((X - 0.5) ** 2 + (Y - 0.45) ** 2) / 0.01)
+    z = np.zeros_like(h0)
+    return S.Scenario(name="bump", nx=n, ny=n, extent=((0.0, 1.0), (0.0, 1.0)), B=None, w0=h0, hu0=z, hv0=z.copy(),
+                      cfl=0.2)
+
+
+def time_order(run, T=0.0128, dts_div=(16, 32, 64, 128), ref_div=2048):
+    """Observed order of a stepper in time, as test/test_timesteppers.jl:70-83
+    measures it: errors at T against a fine RK2 reference, fitted in log-log.
+    run(stepper, dt, T) returns w at T."""
+    ref = run("rk2", T / ref_div, T)
+    out = {}
+    for st in ("rk2", "fe"):
+        dts = [T / d for d in dts_div]
+        errs = [float(np.abs(run(st, dt, T) - ref).max()) for dt in dts]
+        out[st] = float(np.polyfit(np.log(dts), np.log(errs), 1)[0])
+    return out
+
+
+def _oracle_run(stepper, dt, T):
+    sc = smooth_bump()
+    sc.stepper = stepper
+    o = oracle_from(sc)
+    for _ in range(int(round(T / dt))):
+        o.perform_step(dt)  # max_dt below the CFL step: every step is exactly dt
+    return o.interior()[0]
+
+
+def test_time_order_of_the_steppers():
+    # test/test_timesteppers.jl:70-87: forward Euler is first order, RK2 second
+    # order in time (here for the full shallow-water right-hand side, fixed dt)
+    order = time_order(_oracle_run)
+    assert order["rk2"] == pytest.approx(2.0, abs=0.05)
+    assert order["fe"] == pytest.approx(1.0, abs=0.1)
