@@ -18,8 +18,9 @@
 // Tiles are TX x TY interior cells; each block stages its tile with a 2-cell
 // halo of (w, hu, hv) and a 2..3-cell halo of bottom corners in shared memory.
 // The Float64 kernels of the per-step path (k_flux_tma, k_stage2_tma) stage
-// them with TMA copies (vf_tma.cuh); the ensemble and Float32 tiles load them
-// with plain loads.
+// them with TMA copies, and the stage pass writes its output tile with a TMA
+// tensor store (vf_tma.cuh); the ensemble and Float32 tiles load and store
+// the plain way.
 #pragma once
 #include "vf_math.cuh"
 #include "vf_tma.cuh"
