@@ -299,6 +299,8 @@ int pump(vf_batch* b) {
       const long long k = w.chunk_end[slot];
       w.head += 1;
       w.inflight -= 1;
+      if (r.wait_fault)
+        return bfail(b, VF_ECUDA, "wide member: a bounded wait for a TMA tile copy gave up");
       if (!r.active[k & 1]) {
         wide_finish(b, w, r, k, vf::kEnsOk);
         break;
