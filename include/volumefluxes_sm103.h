@@ -139,6 +139,20 @@ int vf_get_interior_state(vf_handle* h, void* w, void* hu, void* hv);
  * caller does t += dt as simulate_to_time does (src/simulator.jl:205). */
 int vf_step(vf_handle* h, double max_dt, double t, double* dt_out);
 
+/* Float64 arithmetic of the per-step kernels (vf_step, vf_simulate and the
+ * wide members of a batch). VF_ARITH_REFERENCE (the default): every operation
+ * rounds as the reference's Julia code does, so results equal the reference
+ * CPU path bit for bit. VF_ARITH_FAITHFUL: quotients correct to about one ulp
+ * (a refined hardware reciprocal shared by quotients with one divisor),
+ * library cube roots and fused multiply-adds; the same passes and branches,
+ * held to the 1e-12 relative max-norm tolerance against the reference path
+ * instead of to its bits, and fewer FP64 instructions per cell. Stands in for
+ * nothing in the reference (whose CPU and KernelAbstractions backends both
+ * round every operation); VF_EINVAL for Float32 handles or another mode. */
+#define VF_ARITH_REFERENCE 0
+#define VF_ARITH_FAITHFUL 1
+int vf_set_arithmetic(vf_handle* h, int32_t mode);
+
 /* Stands in for the loop of simulate_to_time (src/simulator.jl:179-212) with
  * the time kept on the device: from t0, step while t < endtime with
  * max_dt = endtime - t when match_endtime (else +Inf), capped by

@@ -222,3 +222,7 @@ def dual_gauge_loss(sim: OracleSim, w, hu, hv, dts, gauges, target, *, B=None, B
     if rc != 0:
         raise ValueError(f"oracle dual run failed ({rc})")
     return loss.value, dloss.value
+
+
+def get_threads() -> int:
+    return load().vfo_get_threads()

@@ -1,10 +1,12 @@
 """Build libvfsm103.so, the sm_103a shallow-water step library, in-tree.
 
-Seven translation units compile in parallel with nvcc and link into one shared
+Eight translation units compile in parallel with nvcc and link into one shared
 library with the CUDA runtime linked statically:
 
   vf_f64.cu  Float64 kernels, -fmad=false (each operation rounds as in Julia);
              tile kernels held to 80 registers (three resident blocks per SM)
+  vf_f64f.cu Float64 per-step kernels with faithful quotients, -fmad=true
+             (VF_ARITH_FAITHFUL; held to a tolerance, not to the bits)
   vf_f32.cu  Float32 kernels, contraction and fast division allowed
   vf_abi.cu  the extern "C" boundary of include/volumefluxes_sm103.h
   vf_noalloc.cu  the allocation-free water-volume entry point
@@ -34,6 +36,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           f"-I{INCLUDE}", f"-I{CSRC}"]
 UNITS = {
     "vf_f64.cu": ["-fmad=false", "-DVF_TILE_MIN_BLOCKS=3"],
+    "vf_f64f.cu": ["-fmad=true", "-DVF_TILE_MIN_BLOCKS=3"],
     "vf_f32.cu": ["-fmad=true", "-ftz=true", "-prec-sqrt=false"],
     "vf_abi.cu": [],
     "vf_noalloc.cu": [],

@@ -539,8 +539,20 @@ int vf_create(const vf_config* cfg, vf_handle** out) {
   h->af.L = static_cast<float*>(h->L);
   h->af.S = static_cast<float*>(h->S);
   h->af.rec = h->rec;
+  h->ad.arith = h->af.arith = VF_ARITH_REFERENCE;
   make_tma_maps(h);
   *out = h;
+  return VF_OK;
+}
+
+int vf_set_arithmetic(vf_handle* h, int32_t mode) {
+  if (!h) return fail(nullptr, VF_EINVAL, "handle is NULL");
+  if (mode != VF_ARITH_REFERENCE && mode != VF_ARITH_FAITHFUL)
+    return fail(h, VF_EINVAL, "arithmetic mode must be VF_ARITH_REFERENCE or VF_ARITH_FAITHFUL");
+  if (h->elem != 8 && mode != VF_ARITH_REFERENCE)
+    return fail(h, VF_EINVAL, "faithful arithmetic is a Float64 mode");
+  h->ad.arith = mode;
+  h->chunk_k = 0;  // a captured step chunk holds the old kernels
   return VF_OK;
 }
 

@@ -118,6 +118,7 @@ int fwd_step(vf_adjoint* a, const void* Uin, void* Uout, double dt) {
   s.L = static_cast<T*>(a->L0);
   s.S = static_cast<T*>(a->S0);
   s.rec = a->rec;
+  s.arith = VF_ARITH_REFERENCE;  // the reverse sweep differentiates the reference-rounded step
   VF_ACK(a, vf::launch_step(s, static_cast<const T*>(Uin), static_cast<T*>(Uout), 0, h->stream));
   h->launches += 2;
   return VF_OK;
@@ -169,6 +170,7 @@ int reverse_step(vf_adjoint* a, const void* U0, double dt) {
   if (int rc = set_dt(a, dt)) return rc;
   vf::StepArgs<T> s = args_of<T>(h);
   s.rec = a->rec;
+  s.arith = VF_ARITH_REFERENCE;
   // recompute L(U0), S(U0), U1, L(U1), S(U1)
   s.L = static_cast<T*>(a->L0);
   s.S = static_cast<T*>(a->S0);

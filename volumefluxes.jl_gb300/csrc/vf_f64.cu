@@ -4,13 +4,17 @@
 #include "vf_step_impl.cuh"
 
 namespace vf {
+// a.arith == 1 hands the step to the faithful-quotient kernels of vf_f64f.cu.
 cudaError_t launch_step(const StepArgs<double>& a, const double* Uin, double* Uout, int parity, cudaStream_t st) {
+  if (a.arith == 1) return vf_faithful_launch_step(&a, Uin, Uout, parity, st);
   return launch_step_impl<double>(a, Uin, Uout, parity, st);
 }
 cudaError_t launch_flux(const StepArgs<double>& a, const double* Uin, int parity, cudaStream_t st) {
+  if (a.arith == 1) return vf_faithful_launch_flux(&a, Uin, parity, st);
   return launch_flux_impl<double>(a, Uin, parity, st);
 }
 cudaError_t launch_stage(const StepArgs<double>& a, const double* Uin, double* Uout, int parity, cudaStream_t st) {
+  if (a.arith == 1) return vf_faithful_launch_stage(&a, Uin, Uout, parity, st);
   return launch_stage_impl<double>(a, Uin, Uout, parity, st);
 }
 cudaError_t launch_bc(const Geom<double>& g, double* U, cudaStream_t st) { return launch_bc_impl<double>(g, U, st); }
@@ -45,5 +49,8 @@ cudaError_t launch_sample(const Geom<double>& g, const double* U, const int* ij,
   k_sample<double><<<(n + 127) / 128, 128, 0, st>>>(g, U, ij, n, out);
   return cudaGetLastError();
 }
-cudaError_t configure_kernels_f64() { return configure_impl<double>(); }
+cudaError_t configure_kernels_f64() {
+  const cudaError_t e = configure_impl<double>();
+  return e != cudaSuccess ? e : vf_faithful_configure();
+}
 }  // namespace vf

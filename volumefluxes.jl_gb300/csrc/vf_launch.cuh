@@ -6,6 +6,15 @@
 #include "vf_ensemble.cuh"
 #include "vf_march.cuh"
 
+// Float64 step kernels with faithful quotients and multiply-add contraction
+// (vf_f64f.cu, a unit whose kernels live in their own namespace). `args` points
+// to a vf::StepArgs<double>; same contract as vf::launch_step / launch_flux /
+// launch_stage.
+cudaError_t vf_faithful_launch_step(const void* args, const double* Uin, double* Uout, int parity, cudaStream_t st);
+cudaError_t vf_faithful_launch_flux(const void* args, const double* Uin, int parity, cudaStream_t st);
+cudaError_t vf_faithful_launch_stage(const void* args, const double* Uin, double* Uout, int parity, cudaStream_t st);
+cudaError_t vf_faithful_configure();
+
 namespace vf {
 
 template <typename T>
@@ -19,6 +28,7 @@ struct StepArgs {
   T* S;
   StepRecord* rec;
   TmaMaps tma;  // Float64 tile kernels: TMA staging when tma.ok and the buffers match
+  int arith;    // Float64 per-step kernels: 0 rounded as the reference, 1 faithful quotients (vf_f64f.cu)
 };
 
 // One full step reading Uin, writing Uout; parity selects the record slot.

@@ -16,26 +16,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include "vf_idiv.cuh"
-#include "vf_sdiv.cuh"
 
-// Float64 division on the integer pipe (1) or the FP64 pipe (0). Both are
-// correctly rounded. Measured on the 4096^2 wet/dry step the integer-pipe
-// division was slower (40.0 vs 31.5 ms/step: it raises registers from 80 to
-// 114 per thread and halves the resident blocks), so the FP64 pipe is the
-// default and the integer path stays as a build option.
-#ifndef VF_FP64_INT_DIV
-#define VF_FP64_INT_DIV 0
-#endif
-// Float64 quotients sharing a divisor through one refined reciprocal and an
-// exact rounding test (1), or one IEEE division each (0); both are exact.
-// Measured on GB300 the shared form is slower: 32 G quotients/s against 56-59
-// for the hardware division in a throughput test (four quotients per divisor,
-// every one on the fast path, bitwise equal), and 41.1 vs 31.0 ms per 4096^2
-// wet/dry step, so one division each is the default.
-#ifndef VF_FP64_SHARED_DIV
-#define VF_FP64_SHARED_DIV 0
-#endif
 // Float32 reciprocals and cube roots from the special-function unit (1:
 // rcp.approx, and cbrt(x) = 2^(log2|x| / 3) with the sign of x; a few ulps) or
 // the correctly rounded reciprocal and the libm cube root (0). Float32 results
@@ -44,6 +25,16 @@
 // special-function unit, 1.069 ms without.
 #ifndef VF_F32_FAST_SFU
 #define VF_F32_FAST_SFU 1
+#endif
+// Float64 quotients correct to about one ulp instead of correctly rounded (1),
+// for the tolerance-bound Float64 kernels (vf_f64f.cu, built with multiply-add
+// contraction): a reciprocal from the hardware approximation refined by one
+// third-order Newton step, a quotient a/b as a * (1/b) plus one residual
+// correction, and quotients that share a divisor as products with one shared
+// reciprocal. Cube roots come from the CUDA math library. 0: every operation
+// rounds as in the reference (the bitwise kernels).
+#ifndef VF_FP64_FAITHFUL
+#define VF_FP64_FAITHFUL 0
 #endif
 
 namespace vf {
@@ -58,7 +49,7 @@ struct Arith;
 // divisor is bounded away from zero).
 template <>
 struct Arith<double> {
-  static constexpr bool exact = true;
+  static constexpr bool exact = !VF_FP64_FAITHFUL;
   static __device__ __forceinline__ long long bits(double x) { return __double_as_longlong(x); }
   // Monotone key: orders all non-NaN doubles, with -0.0 just below +0.0.
   static __device__ __forceinline__ long long key(double x) {
@@ -82,39 +73,44 @@ struct Arith<double> {
   // Julia's max/min: -0.0 < +0.0.
   static __device__ __forceinline__ double max(double x, double y) { return key(x) > key(y) ? x : y; }
   static __device__ __forceinline__ double min(double x, double y) { return key(x) < key(y) ? x : y; }
-  // Correctly rounded division: IEEE on the FP64 pipe, or (VF_FP64_INT_DIV)
-  // on the integer pipe (vf_idiv.cuh) with the FP64 pipe only for operands
-  // or results outside the normal range.
-  static __device__ __forceinline__ double div(double a, double b) {
-#if VF_FP64_INT_DIV
-    double q;
-    return idiv_normal(a, b, &q) ? q : a / b;
-#else
-    return a / b;
-#endif
+#if VF_FP64_FAITHFUL
+  // Reciprocal: the hardware approximation r0 (rcp.approx.ftz.f64, relative
+  // error e0) refined by one third-order Newton step r0 * (1 + e + e^2) with
+  // e = 1 - b*r0, whose error is e0^3 plus the rounding of the last fused
+  // multiply-add. Divisors on this path are normal numbers (desingularised
+  // depths >= kappa/2, wave-speed spreads >= kappa, 1 - dt*S >= 1).
+  static __device__ __forceinline__ double rcp(double b) {
+    double r0;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r0) : "d"(b));
+    const double e = fma(-b, r0, 1.0);
+    return fma(r0, fma(e, e, e), r0);
   }
+  // a/b as q = a * (1/b) corrected once by the exact residual a - b*q.
+  static __device__ __forceinline__ double div(double a, double b) {
+    const double r = rcp(b);
+    const double q = a * r;
+    return fma(fma(-b, q, a), r, q);
+  }
+  static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
+  struct Recip {
+    double r;
+  };
+  static __device__ __forceinline__ Recip recip(double b) { return Recip{rcp(b)}; }
+  static __device__ __forceinline__ double div_by(const Recip& R, double a) { return a * R.r; }
+#else
+  // Correctly rounded division and square root on the FP64 pipe. (Measured on
+  // the 4096^2 wet/dry step and not kept: a correctly rounded division on the
+  // integer pipe, 40.0 vs 31.5 ms per step, and quotients sharing one refined
+  // reciprocal with an exact rounding test, 41.1 vs 31.0 ms.)
+  static __device__ __forceinline__ double div(double a, double b) { return a / b; }
   static __device__ __forceinline__ double rcp(double b) { return 1.0 / b; }
   static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
-  // Several quotients over one divisor, each still IEEE a/b (vf_sdiv.cuh).
-  using Recip = SharedRecip;
-  static __device__ __forceinline__ Recip recip(double b) {
-#if VF_FP64_SHARED_DIV
-    return sd_recip(b);
-#else
-    SharedRecip R;
-    R.b = b;
-    R.y = 0.0;
-    R.eb = 0;
-    return R;
-#endif
-  }
-  static __device__ __forceinline__ double div_by(const Recip& R, double a) {
-#if VF_FP64_SHARED_DIV
-    return sd_div(R, a);
-#else
-    return div(a, R.b);
-#endif
-  }
+  struct Recip {
+    double b;
+  };
+  static __device__ __forceinline__ Recip recip(double b) { return Recip{b}; }
+  static __device__ __forceinline__ double div_by(const Recip& R, double a) { return a / R.b; }
+#endif  // VF_FP64_FAITHFUL
 };
 
 template <>
@@ -163,16 +159,9 @@ __device__ __forceinline__ int cmp192(uint64_t a0, uint64_t a1, uint64_t a2, uin
   return 0;
 }
 
-// Out of line by default (the friction law calls it from two places per cell
-// and step); VF_CBRT_INLINE=1 inlines it.
-#ifndef VF_CBRT_INLINE
-#define VF_CBRT_INLINE 0
-#endif
-#if VF_CBRT_INLINE
-static __device__ __forceinline__ double cr_cbrt(double x) {
-#else
+// Out of line: the friction law calls it from two places per cell and step
+// (inlined it measured 31.06 vs 31.00 ms per 4096^2 wet/dry step).
 static __device__ __noinline__ double cr_cbrt(double x) {
-#endif
   if (x == 0.0 || !isfinite(x)) return x;
   const bool neg = signbit(x);
   double a = fabs(x);
@@ -219,7 +208,11 @@ static __device__ __noinline__ double cr_cbrt(double x) {
 }
 
 template <typename T> __device__ __forceinline__ T vcbrt(T x);
+#if VF_FP64_FAITHFUL
+template <> __device__ __forceinline__ double vcbrt<double>(double x) { return cbrt(x); }
+#else
 template <> __device__ __forceinline__ double vcbrt<double>(double x) { return cr_cbrt(x); }
+#endif
 #if VF_F32_FAST_SFU
 template <> __device__ __forceinline__ float vcbrt<float>(float x) {
   float y;

@@ -22,12 +22,13 @@ VF_FRICTION_NONE, VF_FRICTION_BSA2012, VF_FRICTION_FCG2016, VF_FRICTION_BH2021 =
 VF_STEPPER_FE, VF_STEPPER_RK2 = 1, 2
 VF_BC_WALL, VF_BC_PERIODIC, VF_BC_NEUMANN = 1, 2, 3
 VF_REC_LINEAR, VF_REC_NONE = 1, 2
+VF_ARITH_REFERENCE, VF_ARITH_FAITHFUL = 0, 1
 
 # Every symbol include/volumefluxes_sm103.h declares.
 EXPORTED_SYMBOLS = (
     "vf_create", "vf_destroy", "vf_upload_bottom", "vf_set_source_table", "vf_set_source_field",
     "vf_set_interior_state", "vf_upload_state",
-    "vf_download_state", "vf_get_interior_state", "vf_step", "vf_simulate", "vf_water_volume",
+    "vf_download_state", "vf_get_interior_state", "vf_step", "vf_set_arithmetic", "vf_simulate", "vf_water_volume",
     "vf_device_state", "vf_stream", "vf_time_steps", "vf_time_kernels", "vf_selftest_tile_wait", "vf_last_error",
     "vf_launch_count",
     "vf_water_volume_static",
@@ -108,6 +109,7 @@ def load(build_if_missing: bool = False):
         "vf_download_state": (C.c_int, [H, C.c_void_p]),
         "vf_get_interior_state": (C.c_int, [H, C.c_void_p, C.c_void_p, C.c_void_p]),
         "vf_step": (C.c_int, [H, C.c_double, C.c_double, C.POINTER(C.c_double)]),
+        "vf_set_arithmetic": (C.c_int, [H, C.c_int32]),
         "vf_set_source_table": (C.c_int, [H, C.c_int32, C.c_void_p, C.c_void_p, C.c_int32]),
         "vf_set_source_field": (C.c_int, [H, C.c_int32, C.c_void_p]),
         "vf_simulate": (C.c_int, [H, C.c_double, C.c_double, C.c_int32, C.c_double, C.c_double, C.c_int64,

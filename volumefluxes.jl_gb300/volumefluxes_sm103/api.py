@@ -429,14 +429,24 @@ class SM103Backend:
 
     Stands beside KernelAbstractionBackend (src/backends/kernel_abstractions.jl:29-40);
     `realtype` is np.float64 or np.float32, `device` a CUDA ordinal.
+    `arithmetic` (Float64 only): "reference" rounds every operation as the
+    reference does (results equal its CPU path bit for bit); "faithful" uses
+    faithful quotients and fused multiply-adds in the per-step kernels, held
+    to 1e-12 relative max-norm against the reference path instead of to its
+    bits.
     """
 
-    def __init__(self, realtype=np.float64, device: int = 0):
+    def __init__(self, realtype=np.float64, device: int = 0, arithmetic: str = "reference"):
         rt = np.dtype(realtype)
         if rt not in (np.dtype(np.float64), np.dtype(np.float32)):
             raise ArgumentError("realtype must be float64 or float32")
+        if arithmetic not in ("reference", "faithful"):
+            raise ArgumentError("arithmetic must be 'reference' or 'faithful'")
+        if arithmetic == "faithful" and rt != np.dtype(np.float64):
+            raise ArgumentError("faithful arithmetic is a Float64 mode")
         self.realtype = rt.type
         self.device = int(device)
+        self.arithmetic = arithmetic
 
 
 def name(backend) -> str:
@@ -621,6 +631,8 @@ class Simulator:
         h = C.c_void_p()
         N.check(self._lib, None, self._lib.vf_create(C.byref(cfg), C.byref(h)))
         self._h = h
+        if getattr(backend, "arithmetic", "reference") == "faithful":
+            N.check(self._lib, self._h, self._lib.vf_set_arithmetic(self._h, N.VF_ARITH_FAITHFUL))
         eqB = system.equation.B
         if isinstance(eqB, BottomTopography2D):
             B = np.ascontiguousarray(np.asarray(eqB.B, dtype=self.dtype).T)

@@ -139,20 +139,53 @@ def circular_dam_break(n: int = 256, radius: float = 0.15, cfl: float = 0.2) -> 
                     hu0=z, hv0=z.copy(), cfl=cfl)
 
 
+_LN2_HI = float.fromhex("0x1.62e42fee00000p-1")  # ln 2 to 32 bits: kd * _LN2_HI is exact for |kd| < 2^20
+_LN2_LO = float.fromhex("0x1.a39ef35793c76p-33")  # ln 2 - _LN2_HI
+_INV_FACT = [1.0]
+for _n in range(1, 15):
+    _INV_FACT.append(_INV_FACT[-1] / _n)
+
+
+def det_exp(x: np.ndarray) -> np.ndarray:
+    """exp(x) for x <= 0 from IEEE +, -, *, / and exact scaling only, so the same
+    bits come out on every machine (numpy's exp is not correctly rounded and its
+    SIMD variants differ between x86 and Arm in the last bit). Cody-Waite
+    reduction x = k ln 2 + r with |r| <= ln 2 / 2 and a two-part ln 2, then the
+    Taylor series of exp(r) to degree 14 in Horner form, then ldexp by k; within
+    a few ulp of exp."""
+    x = np.asarray(x, dtype=np.float64)
+    kd = np.rint(x * 1.4426950408889634)  # nearest double to 1/ln 2
+    kd = np.maximum(kd, -1100.0)
+    r = (x - kd * _LN2_HI) - kd * _LN2_LO
+    q = np.full_like(r, _INV_FACT[14])
+    for n in range(13, -1, -1):
+        q = q * r + _INV_FACT[n]
+    out = np.ldexp(q, kd.astype(np.int64))
+    return np.where(x < -745.0, 0.0, out)
+
+
 def hill_bottom(nx: int, ny: int, extent, n_hills: int, seed: int, slope: float = 1e-3,
                 amp=(0.5, 4.0), width=(50.0, 400.0)) -> np.ndarray:
+    """Corner bottom (nx+5, ny+5): slope * x plus n_hills Gaussian hills
+    a * exp(-(x-cx)^2 / (2 s^2)) * exp(-(y-cy)^2 / (2 s^2)), centres uniform in the
+    domain, a ~ U[amp], s ~ U[width], drawn from splitmix64(seed). Each hill is
+    the outer product of two 1D Gaussians evaluated with det_exp, so the terrain
+    is bit-for-bit the same on every machine."""
     grid = vf.CartesianGrid(nx, ny, gc=2, boundary=vf.WallBC(), extent=[list(extent[0]), list(extent[1])])
-    f = vf.cell_faces(grid, interior=False)
-    x, y = f[:, :, 0], f[:, :, 1]
+    xv = vf.cell_faces(grid, 1, interior=False)
+    yv = vf.cell_faces(grid, 2, interior=False)
     rng = SplitMix64(seed)
     (x0, x1), (y0, y1) = extent
-    B = slope * x
+    B = slope * np.broadcast_to(xv[:, None], (xv.size, yv.size))
     for _ in range(n_hills):
         cx = rng.uniform(x0, x1)
         cy = rng.uniform(y0, y1)
         a = rng.uniform(*amp)
         s = rng.uniform(*width)
-        B = B + a * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2.0 * s * s))
+        two_s2 = 2.0 * s * s
+        ex = det_exp(-((xv - cx) * (xv - cx)) / two_s2)
+        ey = det_exp(-((yv - cy) * (yv - cy)) / two_s2)
+        B = B + (a * ex)[:, None] * ey[None, :]
     return B
 
 
