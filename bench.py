@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--n", "--grid", dest="n", type=int, default=4096, help="side of the square grid")
     ap.add_argument("--dtype", choices=("f64", "f32"), default="f64")
     ap.add_argument("--no-variant", action="store_true", help="skip the Float32 variant")
+    ap.add_argument("--no-faithful", action="store_true", help="skip the faithful-arithmetic Float64 variant")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--start-steps", type=int, default=0,
@@ -62,18 +63,22 @@ def parse():
                     help="seconds of oracle stepping the reference arm may spend (it runs min(K, budget) steps)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--ensemble-members", type=int, default=256)
-    ap.add_argument("--ensemble-plain-budget", type=float, default=30.0,
-                    help="seconds the sequential plain baseline of the ensemble may spend (it runs a sample)")
+    ap.add_argument("--ensemble-sample-every", type=int, default=8,
+                    help="the plain baseline runs every m-th member (all of them), and so does a batch of that sample")
     ap.add_argument("--no-autotune", action="store_true", help="ensemble with the library's default granularity")
     ap.add_argument("--ensemble-wide-cells", type=int, default=None,
                     help="members with at least this many cells run the whole-grid kernels (default: autotuned)")
     ap.add_argument("--ensemble-endtime-cap", type=float, default=None,
                     help="cap every member's end time (small profiling runs only; the metric uses the full times)")
-    ap.add_argument("--serving", action="store_true", help="also measure the serving loop (adds ~2 min)")
-    ap.add_argument("--serving-requests", type=int, default=48)
+    ap.add_argument("--serving", action="store_true", help="measure the serving loop (the default; ~2 min)")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving loop")
+    ap.add_argument("--serving-requests", type=int, default=24)
     ap.add_argument("--serving-rates", default="10,100,1000", help="Poisson arrival rates [req/s]")
     ap.add_argument("--serving-budget-gb", type=float, default=120.0)
-    ap.add_argument("--adjoint", action="store_true", help="also measure the differentiation workload (~1-2 min)")
+    ap.add_argument("--serving-time-scale", type=float, default=0.1,
+                    help="end times are U[10,600] s times this factor (1.0: the configuration's own times)")
+    ap.add_argument("--adjoint", action="store_true", help="measure the differentiation workload (the default)")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiation workload")
     ap.add_argument("--adjoint-n", type=int, default=512)
     ap.add_argument("--adjoint-steps", type=int, default=400)
     ap.add_argument("--adjoint-fd-dirs", type=int, default=64)
@@ -232,6 +237,14 @@ def workload_name(sc, dtype):
             f"w=max(1.5,B), Manning n=0.03 (bsa2012), rain 1e-5 m/s, infiltration 2e-6 m/s, wall BCs, CFL 0.25")
 
 
+def bench_config(sc, dtype, world):
+    """The `config` object of both arms' lines (identical keys and values)."""
+    cells = sc.nx * sc.ny
+    return {"workload": workload_name(sc, dtype), "nx": sc.nx, "ny": sc.ny, "seed": sc.meta["seed"],
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "inputs larger than L2 (state %.0f MB per volume)" % (3 * cells * (8 if dtype == "f64" else 4) / 1e6)}
+
+
 def run_reference(args):
     world, rank, local = dist_setup("gloo")
     if rank != 0:
@@ -245,7 +258,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
         "steps": steps, "warmup": args.warmup, "ms_per_step": el / steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(sc, "f64"), "nx": sc.nx, "ny": sc.ny, "parallelism": "replicas"},
+        "config": bench_config(sc, "f64", world),
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "VolumeFluxes.jl is Julia and no Julia toolchain exists on the box; the reference arm runs the "
@@ -254,40 +267,96 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def measure_gpu(sc, dtype, args, world, local):
+FULL_STEPS = 1000        # the configuration's run length
+FD_EPS = 1e-7            # central-difference step of the gradient check
+DEVELOPED_STEPS = 20     # per-kernel timing window after the full run (the developed flow)
+
+
+def _time_steps(sim, n):
     import ctypes as C
     import volumefluxes_sm103 as vf
-    real = np.float64 if dtype == "f64" else np.float32
     ms = C.c_float()
-    if args.warmup > 0:  # warm-up on a throwaway simulator; the timed run starts from the initial state
-        warm = sc.build(vf.SM103Backend(real, device=local))
-        vf._native.check(warm._lib, warm.handle, warm._lib.vf_time_steps(warm.handle, args.warmup, C.byref(ms)))
+    vf._native.check(sim._lib, sim.handle, sim._lib.vf_time_steps(sim.handle, int(n), C.byref(ms)))
+    return float(ms.value)
+
+
+def _time_kernels(sim, n):
+    import ctypes as C
+    import volumefluxes_sm103 as vf
+    mf, mst = C.c_float(), C.c_float()
+    vf._native.check(sim._lib, sim.handle, sim._lib.vf_time_kernels(sim.handle, int(n), C.byref(mf), C.byref(mst)))
+    return mf.value / n, mst.value / n
+
+
+def _state(sim):
+    import volumefluxes_sm103 as vf
+    g = vf.current_interior_state(sim)
+    return tuple(np.asarray(a, dtype=np.float64) for a in (g.h, g.hu, g.hv))
+
+
+def measure_gpu(sc, dtype, args, world, local, arithmetic="reference"):
+    """Device throughput of one precision (and Float64 arithmetic mode).
+
+    headline: K steps back to back from the initial state (after W warm-up
+    steps on a throwaway simulator), CUDA events on the library's stream.
+    kernels: the same K steps on a second simulator with events between the
+    two kernels of every step. full: when K < 1000 (the configuration's run)
+    the 1000 steps on a third simulator. developed: per-kernel times of the 20
+    steps after step 1000, the developed flow the ncu captures describe."""
+    import volumefluxes_sm103 as vf
+    real = np.float64 if dtype == "f64" else np.float32
+    be = vf.SM103Backend(real, device=local, arithmetic=arithmetic)
+    if args.warmup > 0:
+        warm = sc.build(be)
+        _time_steps(warm, args.warmup)
         warm.close()
-    sim = sc.build(vf.SM103Backend(real, device=local))
-    lib = sim._lib
+    sim = sc.build(be)
     if args.start_steps > 0:
-        vf._native.check(lib, sim.handle, lib.vf_time_steps(sim.handle, args.start_steps, C.byref(ms)))
+        _time_steps(sim, args.start_steps)
     if args.state_out:
         st = vf.current_interior_state(sim)
         np.savez(args.state_out, h=st.h, hu=st.hu, hv=st.hv)
         sys.exit(0)
-    # headline: K steps back to back, CUDA events on the library's stream
     barrier(world)
     n0 = sim.launch_count()
     with Clocks(local) as clk:
-        vf._native.check(lib, sim.handle, lib.vf_time_steps(sim.handle, args.steps, C.byref(ms)))
+        ms = _time_steps(sim, args.steps)
     launches = sim.launch_count() - n0
     barrier(world)
-    ms_total = allmax(world, float(ms.value))
-    # per-kernel durations (events between the two kernels of every step), on a
-    # second run over the same steps from the same initial state
-    prof = sc.build(vf.SM103Backend(real, device=local))
+    ms_total = allmax(world, ms)
+    out = {"sim": sim, "ms_total": ms_total, "launches": launches, "clocks": clk.summary(), "state": _state(sim)}
+    prof = sc.build(be)
     if args.start_steps > 0:
-        vf._native.check(lib, prof.handle, lib.vf_time_steps(prof.handle, args.start_steps, C.byref(ms)))
-    mf, mst = C.c_float(), C.c_float()
-    vf._native.check(lib, prof.handle, lib.vf_time_kernels(prof.handle, args.steps, C.byref(mf), C.byref(mst)))
+        _time_steps(prof, args.start_steps)
+    out["ms_flux"], out["ms_stage"] = _time_kernels(prof, args.steps)
     prof.close()
-    return sim, ms_total, mf.value / args.steps, mst.value / args.steps, launches, clk.summary()
+    if args.start_steps == 0 and args.steps < FULL_STEPS:
+        full = sc.build(be)
+        out["full_ms"] = _time_steps(full, FULL_STEPS)
+        out["full_state"] = _state(full)
+    elif args.start_steps == 0 and args.steps == FULL_STEPS:
+        full = None
+        out["full_ms"] = ms_total
+        out["full_state"] = out["state"]
+    else:
+        full = None
+    if "full_ms" in out:
+        dev = full if full is not None else sim
+        out["dev_flux"], out["dev_stage"] = _time_kernels(dev, DEVELOPED_STEPS)
+        if full is not None:
+            full.close()
+    return out
+
+
+def field_errors(got, ref):
+    """Max-norm errors of (w, hu, hv) against a reference state: per field
+    relative to the field's own max-norm, and relative to max |w|."""
+    scale_w = float(np.abs(ref[0]).max())
+    out = {}
+    for name, a, b in zip(("w", "hu", "hv"), got, ref):
+        d = float(np.abs(a - b).max())
+        out[name] = {"max_abs": d, "rel_field": d / max(float(np.abs(b).max()), 1e-300), "rel_state": d / scale_w}
+    return out
 
 
 def e2e_rate(sim, steps: int):
@@ -329,17 +398,23 @@ def roofline(sc, dtype, ms_flux, ms_stage, peak, peak_kind, traffic):
     }
 
 
-def fp64_roofline(sc, ms_flux, ms_stage, clk_mhz, inst):
-    """Compute bound of the Float64 kernels: FP64-pipe thread instructions per second vs the pipe's peak."""
+def fp64_roofline(sc, ms_stage_developed, clk_mhz, inst):
+    """Compute bound of the Float64 stage pass in the developed flow: FP64-pipe
+    thread instructions per second against the pipe's peak. The instruction
+    count per cell comes from the ncu capture of a developed-flow launch, so it
+    is applied to the stage pass's time in the same flow state (the steps after
+    step 1000), never to an early window (at rest, friction is skipped and far
+    fewer instructions run)."""
     n = inst.get(("stage", "f64"))
-    if n is None:
+    if n is None or ms_stage_developed is None:
         return None
     cells = sc.nx * sc.ny
-    ach = n * cells / (ms_stage * 1e-3)
+    ach = n * cells / (ms_stage_developed * 1e-3)
     peak = FP64_INST_PER_CLK_SM * N_SMS * (clk_mhz or 2070.0) * 1e6
     return {"bound": "fp64_pipe", "kernel": kernel_names("f64")["stage"], "achieved": ach, "peak": peak,
-            "unit": "FP64 thread-inst/s", "frac": ach / peak, "inst_per_cell": n,
-            "inst_source": "ncu DADD+DMUL+DFMA per cell, 3072^2 developed-flow capture"}
+            "unit": "FP64 thread-inst/s", "frac": ach / peak, "inst_per_cell": n, "launch_ms": ms_stage_developed,
+            "window": f"the {DEVELOPED_STEPS} steps after step {FULL_STEPS} (developed flow)",
+            "inst_source": "ncu DADD+DMUL+DFMA per cell of one stage-pass launch in the developed flow"}
 
 
 def ensemble_workload(n):
@@ -354,10 +429,11 @@ def measure_ensemble(args, local):
 
     Batch: every member from its initial state to its end time in one vf_batch
     launch set, states resident on the device; latency of a member = time from
-    the launch until the host sees its done flag. Plain: simulate_to_time per
-    member, one after the other, on a sample of members (every m-th, time-boxed);
-    the sequential latencies for all members arriving at once are estimated from
-    the sample's mean time per member.
+    the launch until the host sees its done flag. Measured on a sample (every
+    m-th member, all of them): the plain drop-in, simulate_to_time per member
+    one after the other, against the same members as a batch of their own.
+    The plain figures for all members are extrapolated from the sample's mean
+    time per member and labelled as estimates.
     """
     import volumefluxes_sm103 as vf
     from volumefluxes_sm103 import ensemble as E
@@ -409,42 +485,80 @@ def measure_ensemble(args, local):
         "options": None if tuned is None else {k: v for k, v in tuned.__dict__.items() if v is not None},
         "autotune_top": [[{k: v for k, v in c.__dict__.items() if v is not None}, r] for c, r in table[:4]],
     }
-    # the plain drop-in, one member after the other, on a time-boxed sample
-    m = 8
-    sample, times, equal = [], [], 0
-    tb = time.perf_counter()
-    for i in range(0, len(scen), m):
-        if time.perf_counter() - tb > args.ensemble_plain_budget:
-            break
+    final_h = [vf.current_interior_state(x).h for x in sims[::args.ensemble_sample_every]]
+    for x in sims:
+        x.close()
+    # the plain drop-in on a sample (every m-th member, all of them): one
+    # simulate_to_time after the other, all arriving at once, served in index
+    # order; and the same sample as a batch of its own
+    m = args.ensemble_sample_every
+    sample = list(range(0, len(scen), m))
+    service, equal = [], 0
+    for k, i in enumerate(sample):
         p = scen[i].build(be)
         t1 = time.perf_counter()
         vf.simulate_to_time(p, ends[i])
-        times.append(time.perf_counter() - t1)
-        sample.append(i)
-        equal += int(np.array_equal(vf.current_interior_state(p).h, vf.current_interior_state(sims[i]).h))
+        service.append(time.perf_counter() - t1)
+        equal += int(np.array_equal(vf.current_interior_state(p).h, final_h[k]))
         p.close()
-    for s in sims:
-        s.close()
-    mean_t = float(np.mean(times))
+    service = np.array(service)
+    plain_lat = np.cumsum(service)
+    sub = [scen[i].build(be) for i in sample]
+    sub_done = [None] * len(sub)
+    t0 = time.perf_counter()
+    run = E.BatchRun(sub, [ends[i] for i in sample], options=tuned)
+    pending = set(range(len(sub)))
+    while pending:
+        for i in list(pending):
+            if run.is_done(i):
+                sub_done[i] = time.perf_counter() - t0
+                pending.discard(i)
+        time.sleep(0.0005)
+    run.finish()
+    sub_make = time.perf_counter() - t0
+    for x in sub:
+        x.close()
+    sub_lat = np.array(sub_done)
+
+    def pct(a):
+        return {"p50": float(np.percentile(a, 50)), "p95": float(np.percentile(a, 95)),
+                "p99": float(np.percentile(a, 99)), "max": float(np.max(a))}
+
+    sampled = {
+        "members": f"{len(sample)} of {len(scen)} (every {m}th, all of them)",
+        "plain_sequential": {"makespan_s": float(service.sum()), "scenarios_per_s": len(sample) / float(service.sum()),
+                             "latency_s": pct(plain_lat),
+                             "cell_updates_per_s": float((cells[sample] * steps[sample]).sum() / service.sum())},
+        "batch": {"makespan_s": sub_make, "scenarios_per_s": len(sample) / sub_make, "latency_s": pct(sub_lat)},
+        "speedup_scenarios_per_s": float(service.sum()) / sub_make,
+        "bitwise_equal_plain_vs_batch": f"{equal} of {len(sample)}",
+        "timing": "both arms measured: plain = simulate_to_time per member, one after the other, all arriving at "
+                  "once (latency = finish time in index order); batch = the same members in one vf_batch launch set",
+    }
+    mean_t = float(service.mean())
     total_est = mean_t * len(scen)
     plain = {
-        "scenarios_per_s": 1.0 / mean_t,
-        "cell_updates_per_s": float((cells[sample] * steps[sample]).sum() / np.sum(times)),
+        "scenarios_per_s_est": 1.0 / mean_t,
         "makespan_s_est": total_est,
         "latency_s_est": {"p50": 0.50 * total_est, "p95": 0.95 * total_est, "p99": 0.99 * total_est},
-        "sample": f"{len(sample)} of {len(scen)} members (every {m}th), simulate_to_time each, "
-                  f"{np.sum(times):.1f} s; all-at-once sequential latencies estimated from the mean per member",
-        "bitwise_equal_to_batch": f"{equal} of {len(sample)}",
+        "estimate": f"all {len(scen)} members one after the other, extrapolated from the measured sample's mean "
+                    f"time per member ({mean_t:.2f} s)",
     }
     return {"workload": ensemble_workload(len(scen)), "dtype": "f32", "members": len(scen), "batch": batch,
-            "plain_sequential": plain, "speedup_scenarios_per_s": batch["scenarios_per_s"] / plain["scenarios_per_s"],
+            "sampled_measured": sampled, "plain_sequential_estimated": plain,
+            "speedup_scenarios_per_s_est": batch["scenarios_per_s"] / plain["scenarios_per_s_est"],
             "timing": "host wall clock from vf_batch_launch to each member's done flag (pinned mapped memory), "
                       "states resident on the device"}
 
 
-def serving_workload(n):
+def serving_workload(n, scale):
+    lo, hi = 10.0 * scale, 600.0 * scale
+    cap = "" if scale == 1.0 else (f" (the configuration's U[10,600] s scaled by {scale:g}: at Float64's rate on this "
+                                   "GPU one full-length pass of these requests takes ~6 min, and the measurement runs "
+                                   "four passes)")
     return (f"serving: {n} flood requests drawn as the ensemble members but with sides log-uniform in [128,2048], "
-            "Float32 or Float64 with probability 1/2, end times U[2,20] s; Poisson arrivals; HBM admission budget")
+            f"Float32 or Float64 with probability 1/2, end times U[{lo:g},{hi:g}] s{cap}; Poisson arrivals; "
+            "HBM admission budget")
 
 
 def measure_serving(args, local):
@@ -462,7 +576,8 @@ def measure_serving(args, local):
     import volumefluxes_sm103 as vf
     from volumefluxes_sm103 import scenarios as S
     from volumefluxes_sm103.serving import Request, Server
-    specs = S.serving_specs(args.serving_requests)
+    scale = args.serving_time_scale
+    specs = S.serving_specs(args.serving_requests, endtime_range=(10.0 * scale, 600.0 * scale))
     reqs = [(S.ensemble_member(r.spec), np.float32 if r.real == "f32" else np.float64, r.spec.endtime)
             for r in specs]
     rates = [float(x) for x in args.serving_rates.split(",") if x]
@@ -470,7 +585,7 @@ def measure_serving(args, local):
     rng = np.random.default_rng(20241204)
     gaps = rng.exponential(1.0, size=len(reqs))
     work = sum(sc.nx * sc.ny for sc, _, _ in reqs)
-    out = {"workload": serving_workload(len(reqs)), "requests": len(reqs),
+    out = {"workload": serving_workload(len(reqs), scale), "requests": len(reqs),
            "f64_requests": sum(r == np.float64 for _, r, _ in reqs), "hbm_budget_bytes": budget, "rates": []}
     # warm the kernels and the pool outside the timing
     with Server(budget, device=local) as srv:
@@ -602,7 +717,7 @@ def measure_adjoint(args, local):
     grid = sc.grid()
     f = vf.cell_faces(grid, interior=False)
     rng = np.random.default_rng(20241206)
-    rel = []
+    rel, stable = [], []
     for k in range(args.adjoint_fd_dirs):
         v = np.zeros_like(sc.B)
         for _ in range(3):
@@ -610,18 +725,22 @@ def measure_adjoint(args, local):
             s = rng.uniform(10.0, 80.0)
             v += rng.standard_normal() * np.exp(-((f[:, :, 0] - cx) ** 2 + (f[:, :, 1] - cy) ** 2) / (2 * s * s))
         vn = float(rng.standard_normal()) * 1e-3
-        eps = 1e-7
-        n0 = sc.manning_n
-        lp = AD.gauge_loss(sc, np.float64, gauges, target, dts, B=sc.B + eps * v, manning_n=n0 + eps * vn)
-        lm = AD.gauge_loss(sc, np.float64, gauges, target, dts, B=sc.B - eps * v, manning_n=n0 - eps * vn)
-        fd = (lp - lm) / (2 * eps)
-        got = float(np.sum(gB * v)) + gCz * 2 * n0 * vn
-        rel.append(abs(fd - got) / max(abs(got), 1e-300))
-    rel = np.array(rel)
+        got = float(np.sum(gB * v)) + gCz * 2 * sc.manning_n * vn
+        fd = [AD.central_difference(sc, np.float64, gauges, target, dts, v, vn, e) for e in (FD_EPS, 4 * FD_EPS)]
+        rel.append(abs(fd[0] - got) / max(abs(got), 1e-300))
+        stable.append(AD.fd_consistent(fd[0], fd[1]))
+    rel, stable = np.array(rel), np.array(stable, dtype=bool)
     if len(rel):
-        out["fd"] = {"directions": len(rel), "eps": 1e-7, "rel_err_median": float(np.median(rel)),
+        out["fd"] = {"directions": len(rel), "eps": FD_EPS, "rel_err_median": float(np.median(rel)),
                      "rel_err_p90": float(np.percentile(rel, 90)), "rel_err_max": float(rel.max()),
                      "within_1e-6": int((rel <= 1e-6).sum()),
+                     "fd_consistent": int(stable.sum()),
+                     "rel_err_max_consistent": float(rel[stable].max()) if stable.any() else None,
+                     "within_1e-6_consistent": int((rel[stable] <= 1e-6).sum()),
+                     "classification": "a direction is FD-consistent when its central differences at eps and "
+                                       "4*eps agree to 1e-7 relative; the others cross branch switches (minmod, "
+                                       "dry faces, the dry clamp) within the step, where the loss is not "
+                                       "differentiable and the difference quotient mixes one-sided slopes",
                      "directions_kind": "sums of 3 random Gaussian bumps (width U[10,80] m) on B plus a random n "
                                         "component"}
     # the oracle on dual numbers (the reference CPU path through ForwardDiff's stand-in)
@@ -673,28 +792,72 @@ def main():
     cells = sc.nx * sc.ny
     dtypes = [args.dtype] + ([] if args.no_variant else [d for d in ("f64", "f32") if d != args.dtype])
     results = {}
-    for dt in dtypes:
-        sim, ms_total, ms_flux, ms_stage, launches, clk = measure_gpu(sc, dt, args, world, local)
+    states = {}
+    modes = [(dt, "reference") for dt in dtypes]
+    if "f64" in dtypes and not args.no_faithful:
+        modes.append(("f64", "faithful"))
+    if "f32" in dtypes and not args.no_faithful:
+        modes.append(("f32", "no_near_dry"))
+    for dt, mode in modes:
+        key = {"reference": dt, "faithful": "f64_faithful", "no_near_dry": "f32_no_near_dry"}[mode]
+        if mode == "no_near_dry":  # every Float32 velocity division by the fast reciprocal
+            os.environ["VF_F32_NEAR_DRY"] = "0"
+        try:
+            m = measure_gpu(sc, dt, args, world, local, arithmetic="faithful" if mode == "faithful" else "reference")
+        finally:
+            os.environ.pop("VF_F32_NEAR_DRY", None)
+        sim, ms_total = m["sim"], m["ms_total"]
         value = world * cells * args.steps / (ms_total * 1e-3)
-        if args.e2e_steps > 0:
+        if args.e2e_steps > 0 and mode == "reference":
             e2e_v, h2d, d2h, _ = e2e_rate(sim, args.e2e_steps)
             e2e_v = world * e2e_v  # replicas
         else:
             e2e_v, h2d, d2h = None, 0, 0
         e = 8 if dt == "f64" else 4
         step_ach = WORDS_PER_CELL_STEP * e * cells / (ms_total / args.steps * 1e-3) / 1e9
-        results[dt] = {
-            "value": value, "ms_per_step": ms_total / args.steps, "gpu_launches": launches, "clocks": clk,
-            "roofline": roofline(sc, dt, ms_flux, ms_stage, peak, peak_kind, traffic),
+        r = {
+            "value": value, "ms_per_step": ms_total / args.steps, "gpu_launches": m["launches"], "clocks": m["clocks"],
+            "roofline": roofline(sc, dt, m["ms_flux"], m["ms_stage"], peak, peak_kind, traffic),
             "roofline_step": {"bound": "hbm", "achieved": step_ach, "peak": peak, "unit": "GB/s",
                               "frac": step_ach / peak, "words_per_cell": WORDS_PER_CELL_STEP},
-            "kernel_ms": {kernel_names(dt)["flux"]: ms_flux, kernel_names(dt)["stage"]: ms_stage},
+            "kernel_ms": {kernel_names(dt)["flux"]: m["ms_flux"], kernel_names(dt)["stage"]: m["ms_stage"]},
             "e2e": {"value": e2e_v, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         }
-        if dt == "f64":
-            results[dt]["compute_roofline"] = fp64_roofline(sc, ms_flux, ms_stage, (clk or {}).get("sm_mhz"),
-                                                            fp64_inst)
+        if mode == "faithful":
+            r["arithmetic"] = "faithful quotients and fused multiply-adds (VF_ARITH_FAITHFUL)"
+        if dt == "f32":
+            r["near_dry_f64_division"] = mode != "no_near_dry"
+        if "full_ms" in m:
+            full_ms = m["full_ms"]
+            r["full_config"] = {
+                "steps": FULL_STEPS, "ms_per_step": full_ms / FULL_STEPS,
+                "value": world * cells * FULL_STEPS / (full_ms * 1e-3), "unit": METRIC,
+                "window": f"the configuration's {FULL_STEPS} RK2 steps from the initial state",
+                "developed_kernel_ms": {kernel_names(dt)["flux"]: m["dev_flux"], kernel_names(dt)["stage"]: m["dev_stage"]},
+                "developed_roofline": roofline(sc, dt, m["dev_flux"], m["dev_stage"], peak, peak_kind, traffic),
+            }
+            if dt == "f64" and mode == "reference":
+                r["compute_roofline"] = fp64_roofline(sc, m["dev_stage"], (m["clocks"] or {}).get("sm_mhz"), fp64_inst)
+        if args.steps < FULL_STEPS:
+            r["window_note"] = (f"{args.steps} steps from the initial state: the flow starts at rest (no friction work "
+                                f"for the first ~15 steps), so this window runs faster per step than the "
+                                f"configuration's {FULL_STEPS} steps; see full_config")
+        states[key] = (m["state"], m.get("full_state"))
+        results[key] = r
         sim.close()
+    # errors against the reference-rounded Float64 run, at the end of each window
+    if "f64" in states:
+        ref_k, ref_full = states["f64"]
+        for key, (st_k, st_full) in states.items():
+            if key == "f64":
+                continue
+            err = {"window_steps": args.steps, "at_window_end": field_errors(st_k, ref_k)}
+            if st_full is not None and ref_full is not None:
+                err["at_step_%d" % FULL_STEPS] = field_errors(st_full, ref_full)
+            err["definition"] = ("max |x - x_f64| per field; rel_field divides by the Float64 field's max-norm, "
+                                 "rel_state by max |w| (the state's max-norm)")
+            results[key]["error_vs_f64"] = err
+    states.clear()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         o = oracle_sim(sc)
@@ -708,10 +871,10 @@ def main():
     ens = serving = None
     if rank == 0 and world == 1 and not args.no_ensemble:
         ens = measure_ensemble(args, local)
-    if rank == 0 and world == 1 and args.serving:
+    if rank == 0 and world == 1 and not args.no_serving:
         serving = measure_serving(args, local)
     adjoint = None
-    if rank == 0 and world == 1 and args.adjoint:
+    if rank == 0 and world == 1 and not args.no_adjoint:
         adjoint = measure_adjoint(args, local)
     if rank != 0:
         return
@@ -720,11 +883,10 @@ def main():
         "metric": METRIC, "value": head["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": args.dtype, "data": "synthetic",
-        "config": {"workload": workload_name(sc, args.dtype), "nx": sc.nx, "ny": sc.ny,
-                   "seed": sc.meta["seed"], "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs larger than L2 (state %.0f MB per volume)" % (3 * cells * (8 if args.dtype == 'f64' else 4) / 1e6)},
+        "config": bench_config(sc, args.dtype, world),
         "roofline": head["roofline"], "roofline_step": head["roofline_step"], "kernel_ms": head["kernel_ms"],
-        "compute_roofline": head.get("compute_roofline"),
+        "compute_roofline": head.get("compute_roofline"), "full_config": head.get("full_config"),
+        "window_note": head.get("window_note"),
         "cpu_baseline": cpu, "e2e": head["e2e"], "gpu_launches": head["gpu_launches"], "clocks": head["clocks"],
         "variants": {k: v for k, v in results.items() if k != args.dtype},
         "ensemble": ens,

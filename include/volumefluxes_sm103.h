@@ -363,9 +363,11 @@ const char* vf_adjoint_last_error(vf_adjoint* a);
  *
  * Returns VF_EINVAL for ny > VF_STATIC_MAX_ROWS or bad arguments (message
  * from vf_last_error(NULL)). All calls share the scratch array, which keeps the
- * last call's contents: calls whose kernels overlap on the GPU race. The first
- * call on a device looks the array up with cudaGetSymbolAddress; make it before
- * any stream capture. */
+ * last call's contents: calls whose kernels overlap on the GPU race. A call
+ * outside stream capture looks the array up with cudaGetSymbolAddress (its
+ * address changes when the device or its primary context is reset); a call
+ * during capture reuses the last address found on that device. Make one call
+ * on a device before any capture, and again after a reset of the device. */
 int vf_water_volume_static(const void* state_dev, const void* B_dev, int32_t nx, int32_t ny, int32_t gc,
                            int32_t real_bytes, double dx, double dy, int32_t bottom_is_constant,
                            double bottom_constant, double* out_dev, void* stream);

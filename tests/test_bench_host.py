@@ -6,6 +6,7 @@ import subprocess
 import sys
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -45,10 +46,21 @@ def test_roofline_arithmetic():
 def test_fp64_pipe_roofline():
     sc = scenarios.Scenario(name="t", nx=100, ny=100, extent=((0.0, 1.0), (0.0, 1.0)), B=None,
                             w0=None, hu0=None, hv0=None, cfl=0.25)
-    r = bench.fp64_roofline(sc, 1.0, 2.0, 2000.0, {("stage", "f64"): 500.0})
+    r = bench.fp64_roofline(sc, 2.0, 2000.0, {("stage", "f64"): 500.0})
     assert r["achieved"] == pytest.approx(500.0 * 1e4 / 2e-3)
     assert r["peak"] == pytest.approx(bench.FP64_INST_PER_CLK_SM * bench.N_SMS * 2000.0e6)
-    assert bench.fp64_roofline(sc, 1.0, 2.0, 2000.0, {}) is None
+    assert "developed" in r["window"]
+    assert bench.fp64_roofline(sc, 2.0, 2000.0, {}) is None
+    assert bench.fp64_roofline(sc, None, 2000.0, {("stage", "f64"): 500.0}) is None
+
+
+def test_field_errors():
+    ref = (np.array([[2.0, 4.0]]), np.array([[0.001, -0.002]]), np.zeros((1, 2)))
+    got = (np.array([[2.0, 4.0 + 4e-12]]), np.array([[0.001, -0.002 + 2e-12]]), np.zeros((1, 2)))
+    e = bench.field_errors(got, ref)
+    assert e["w"]["rel_field"] == pytest.approx(1e-12) and e["w"]["rel_state"] == pytest.approx(1e-12)
+    assert e["hu"]["rel_field"] == pytest.approx(1e-9) and e["hu"]["rel_state"] == pytest.approx(5e-13)
+    assert e["hv"]["max_abs"] == 0.0
 
 
 def test_kernel_names_follow_the_switches(monkeypatch):
@@ -76,3 +88,5 @@ def test_reference_arm_prints_its_line():
     line = json.loads(out.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["metric"] == "cell-updates/s" and line["value"] > 0
     assert line["cpu_baseline"]["cores"] >= 1 and line["e2e"]["h2d_bytes_per_step"] == 0
+    # the same config object as the library's arm prints for this workload
+    assert line["config"] == bench.bench_config(scenarios.hills_wet_dry(64), "f64", 1)

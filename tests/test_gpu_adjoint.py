@@ -62,33 +62,57 @@ def test_checkpoint_interval_does_not_change_the_gradient():
     assert a[4] == b[4] == c[4]
 
 
+FD_TOL = 1e-6  # relative agreement of the gradient with central differences
+
+
 def test_cz_gradient_matches_central_differences():
     case, gauges, steps = small_case()
     dts, target, loss, gB, gCz = run_adjoint(case, gauges, steps)
     n = case.scenario.manning_n
-    Cz = n * n
-    eps = 1e-5 * Cz
-    lp = AD.gauge_loss(case.scenario, np.float64, gauges, target, dts, manning_n=math.sqrt(Cz + eps))
-    lm = AD.gauge_loss(case.scenario, np.float64, gauges, target, dts, manning_n=math.sqrt(Cz - eps))
-    fd = (lp - lm) / (2 * eps)
-    # finite differences also see the minmod switches the perturbation crosses,
-    # so they agree only to ~1e-6; the dual-number check above is the exact one
-    assert abs(fd - gCz) <= 1e-5 * abs(gCz), (fd, gCz)
+    zero = np.zeros_like(case.scenario.B)
+    # along n alone: d loss/d n = 2n dLoss/dCz
+    fd = [AD.central_difference(case.scenario, np.float64, gauges, target, dts, zero, 1.0, e) for e in (1e-7, 4e-7)]
+    assert AD.fd_consistent(*fd), fd
+    got = gCz * 2 * n
+    assert abs(fd[0] - got) <= FD_TOL * abs(got), (fd, got)
 
 
 def test_smooth_bottom_direction_matches_central_differences():
     case, gauges, steps = small_case()
     dts, target, loss, gB, gCz = run_adjoint(case, gauges, steps)
     sc = case.scenario
-    grid = sc.grid()
-    f = vf.cell_faces(grid, interior=False)
+    f = vf.cell_faces(sc.grid(), interior=False)
     v = np.exp(-((f[:, :, 0] - 17.0) ** 2 + (f[:, :, 1] - 23.0) ** 2) / (2 * 8.0 ** 2))  # a smooth bump
-    eps = 1e-7
-    lp = AD.gauge_loss(sc, np.float64, gauges, target, dts, B=sc.B + eps * v)
-    lm = AD.gauge_loss(sc, np.float64, gauges, target, dts, B=sc.B - eps * v)
-    fd = (lp - lm) / (2 * eps)
+    fd = [AD.central_difference(sc, np.float64, gauges, target, dts, v, 0.0, e) for e in (1e-7, 4e-7)]
+    assert AD.fd_consistent(*fd), fd
     got = float(np.sum(gB * v))
-    assert abs(fd - got) <= 1e-5 * abs(got), (fd, got)
+    assert abs(fd[0] - got) <= FD_TOL * abs(got), (fd, got)
+
+
+def test_random_directions_match_central_differences_where_differentiable():
+    """16 random directions (Gaussian bumps on B plus an n component): wherever
+    central differences at eps and 4 eps agree (no branch switch inside the
+    step) the gradient matches them to 1e-6; directions that cross a minmod,
+    dry-face or dry-clamp switch are counted, and must stay a minority."""
+    case, gauges, steps = small_case()
+    dts, target, loss, gB, gCz = run_adjoint(case, gauges, steps)
+    sc = case.scenario
+    f = vf.cell_faces(sc.grid(), interior=False)
+    rng = np.random.default_rng(7)
+    consistent = 0
+    for k in range(16):
+        v = np.zeros_like(sc.B)
+        for _ in range(3):
+            cx, cy, s = rng.uniform(0, sc.nx), rng.uniform(0, sc.ny), rng.uniform(3.0, 15.0)
+            v += rng.standard_normal() * np.exp(-((f[:, :, 0] - cx) ** 2 + (f[:, :, 1] - cy) ** 2) / (2 * s * s))
+        vn = float(rng.standard_normal()) * 1e-3
+        fd = [AD.central_difference(sc, np.float64, gauges, target, dts, v, vn, e) for e in (1e-7, 4e-7)]
+        if not AD.fd_consistent(*fd):
+            continue
+        consistent += 1
+        got = float(np.sum(gB * v)) + gCz * 2 * sc.manning_n * vn
+        assert abs(fd[0] - got) <= FD_TOL * abs(got), (k, fd, got)
+    assert consistent >= 12, consistent
 
 
 def test_float32_gradient_tracks_float64():

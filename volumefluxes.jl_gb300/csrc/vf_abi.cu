@@ -127,6 +127,10 @@ void fill_phys(const vf_handle* h, vf::Phys<T>& p) {
   p.dx_pow2 = std::frexp(dx, &ex) == 0.5 ? 1 : 0;
   p.dy_pow2 = std::frexp(dy, &ex) == 0.5 ? 1 : 0;
   p.Cz = (T)c.friction_Cz;
+  // Float32: velocities of cells and faces with |h| < 10 * depth_cutoff are
+  // divided in Float64 (VF_F32_NEAR_DRY=0 turns it off).
+  const char* nd = std::getenv("VF_F32_NEAR_DRY");
+  p.near_dry = (sizeof(T) == 4 && !(nd && std::strcmp(nd, "0") == 0)) ? (T)(10.0 * c.depth_cutoff) : (T)0;
   p.friction = c.friction;
   p.n_bottom = 0;
   p.n_point = 0;

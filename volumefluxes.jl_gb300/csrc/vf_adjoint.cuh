@@ -139,6 +139,7 @@ __device__ __forceinline__ Phys<Dual<T>> dual_phys(const Phys<T>& p) {
   q.dx_pow2 = p.dx_pow2;
   q.dy_pow2 = p.dy_pow2;
   q.Cz = p.Cz;
+  q.near_dry = p.near_dry;
   q.friction = p.friction;
   q.n_bottom = p.n_bottom;
   q.n_point = 0;

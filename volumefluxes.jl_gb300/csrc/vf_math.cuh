@@ -238,6 +238,7 @@ struct Phys {
   T dx, dy;                   // Δx, Δy (src/sourceterms/source_term_bottom.jl:38)
   int dx_pow2, dy_pow2;       // Δ is a power of two: x/Δ == x*(1/Δ) exactly
   T Cz;
+  T near_dry;                 // Float32: |h| below this takes the Float64 velocity division (0: never)
   int friction;               // VF_FRICTION_*
   int n_bottom;               // SourceTermBottom entries
   int n_point;                // rain/infiltration entries, applied in order
@@ -344,15 +345,39 @@ __device__ __forceinline__ T desing(T h, T kappa) {
   return copysign((T)1, h) * A::max(fabs(h), m);
 }
 
+// Desingularised velocities (hu, hv) / h* (src/equations/equation.jl:40-67).
+// A Float32 state divides in Float64 where |h| < p.near_dry (the thin films
+// at wet/dry fronts; out of line, so the common path keeps its registers) and
+// with one fast reciprocal elsewhere; Float64 and dual numbers divide in their
+// own type.
+static __device__ __noinline__ float2 velocity_f64(float hs, float hu, float hv) {
+  const double r = 1.0 / (double)hs;
+  return make_float2((float)((double)hu * r), (float)((double)hv * r));
+}
+template <typename T>
+__device__ __forceinline__ void velocities(const Phys<T>& p, T h, T hs, T hu, T hv, T& u, T& v) {
+  using A = Arith<T>;
+  if constexpr (sizeof(T) == 4) {
+    if (A::abs_lt(h, p.near_dry)) {
+      const float2 uv = velocity_f64(hs, hu, hv);
+      u = uv.x;
+      v = uv.y;
+      return;
+    }
+  }
+  const typename A::Recip R = A::recip(hs);
+  u = A::div_by(R, hu);
+  v = A::div_by(R, hv);
+}
+
 // One side of a face: physical flux (src/equations/swe_2D.jl:43-65) and the
 // two outer eigenvalues (src/equations/swe_2D.jl:69-81).
 template <typename T, int DIR>
 __device__ __forceinline__ void side_flux(const Phys<T>& p, T h, T hu, T hv, T& f0, T& f1, T& f2, T& l1, T& l2) {
   using A = Arith<T>;
   const T hs = desing<T>(h, p.kappa);
-  const typename A::Recip R = A::recip(hs);
-  const T u = A::div_by(R, hu);
-  const T v = A::div_by(R, hv);
+  T u, v;
+  velocities<T>(p, h, hs, hu, hv, u, v);
   const T rh = p.rho * h;
   const T hh = h * h;
   if (DIR == 0) {
@@ -448,10 +473,10 @@ __device__ __forceinline__ bool friction_active(T hu, T hv) {
 template <typename T>
 __device__ __forceinline__ T friction_factor(const Phys<T>& p, T w, T hu, T hv, T Bc) {
   using A = Arith<T>;
-  const T hs = desing<T>(w - Bc, p.kappa);
-  const typename A::Recip R = A::recip(hs);
-  const T u = A::div_by(R, hu);
-  const T v = A::div_by(R, hv);
+  const T h = w - Bc;
+  const T hs = desing<T>(h, p.kappa);
+  T u, v;
+  velocities<T>(p, h, hs, hu, hv, u, v);
   const T speed = A::sqrt_(u * u + v * v);
   T denom;
   if (p.friction == 1) {          // friction_bsa2012

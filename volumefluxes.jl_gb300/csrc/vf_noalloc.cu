@@ -16,8 +16,12 @@
 //    until the process exits;
 //  - every call on a device uses the same array: calls whose kernels overlap
 //    on the GPU (different streams, no ordering between them) race;
-//  - the first call on a device looks the array's address up with that device
-//    current; make that first call before any stream capture.
+//  - a call made outside stream capture looks the array's address up with the
+//    device current (the address can change when the device or its primary
+//    context is reset, e.g. cudaDeviceReset or CUDA.jl's device_reset!, which
+//    reloads the module); a call made during capture uses the address the
+//    last uncaptured call on that device found. So make one call on a device
+//    before capturing, and again after any reset of it.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -56,7 +60,7 @@ __global__ void k_row_volume(const T* __restrict__ state, const T* __restrict__ 
   const int j = gc + blockIdx.x;
   double acc = 0.0;
   for (int i = gc + threadIdx.x; i < gc + nx; i += kThreads) {
-    double Bc = bval;
+    double Bc = (double)(T)bval;  // the constant bottom in the state's type, as vf_water_volume holds it
     if (!bconst) {
       const long long b = (long long)j * (N1 + 1) + i;
       const long long W = N1 + 1;
@@ -76,16 +80,22 @@ __global__ void k_sum_rows(const double* __restrict__ row_sums, int ny, double* 
   if (threadIdx.x == 0) *out = s;
 }
 
-// Address of g_row_sums on the current device, looked up once per device.
-int row_sums_address(double** out) {
+// Address of g_row_sums on the current device. Outside stream capture it is
+// looked up afresh (cheap, and right after a device reset); during capture the
+// last address found on this device is used, since the lookup may load the
+// module, which capture does not allow.
+int row_sums_address(cudaStream_t st, double** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return VF_ECUDA;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  const bool capturing = cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone;
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_row_sums_addr[dev]) {
+  if (!capturing) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_row_sums) != cudaSuccess || !p) return VF_ECUDA;
     g_row_sums_addr[dev] = static_cast<double*>(p);
   }
+  if (!g_row_sums_addr[dev]) return VF_ECUDA;
   *out = g_row_sums_addr[dev];
   return VF_OK;
 }
@@ -111,9 +121,11 @@ extern "C" int vf_water_volume_static(const void* state_dev, const void* B_dev, 
   if (ny > VF_STATIC_MAX_ROWS)
     return fail(VF_EINVAL, "ny exceeds the static scratch capacity of VF_STATIC_MAX_ROWS interior rows");
   if (real_bytes != 8 && real_bytes != 4) return fail(VF_EINVAL, "real_bytes must be 8 or 4");
-  double* rows = nullptr;
-  if (row_sums_address(&rows) != VF_OK) return fail(VF_ECUDA, "cudaGetSymbolAddress of the row-sum scratch failed");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double* rows = nullptr;
+  if (row_sums_address(st, &rows) != VF_OK)
+    return fail(VF_ECUDA, "no address of the row-sum scratch on this device (make one call outside stream capture "
+                          "first; cudaGetSymbolAddress failed or the stream is capturing)");
   const int N1 = nx + 2 * gc;
   if (real_bytes == 8) {
     k_row_volume<double><<<ny, kThreads, 0, st>>>(static_cast<const double*>(state_dev),

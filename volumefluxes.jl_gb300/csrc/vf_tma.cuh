@@ -83,11 +83,29 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
   return done != 0;
 }
 
-// Bounded wait for the phase to complete (each try_wait may suspend the
-// thread for a short, hardware-bounded time); false when it gave up.
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wall-clock limit of one tile-copy wait. A tile copy completes in
+// microseconds; a wait that runs this long has lost its copy. (Kept well
+// above a preemption time slice, so a block that is merely descheduled does
+// not give up; a block that gives up waits once more before it exits, so a
+// lost copy costs it at most twice this.)
+constexpr unsigned long long kTileWaitLimitNs = 50000000ull;  // 50 ms
+
+// Bounded wait for the phase to complete: gives up after `limit` polls or
+// after kTileWaitLimitNs of wall clock (%globaltimer), whichever comes first
+// (each try_wait may suspend the thread for a short, hardware-bounded time);
+// false when it gave up.
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned phase, int limit = 1 << 22) {
-  for (int i = 0; i < limit; ++i)
+  const unsigned long long t0 = globaltimer_ns();
+  for (int i = 0; i < limit; ++i) {
     if (mbar_try_wait(bar, phase)) return true;
+    if ((i & 63) == 63 && globaltimer_ns() - t0 > kTileWaitLimitNs) return false;
+  }
   return false;
 }
 
