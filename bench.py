@@ -82,7 +82,7 @@ def parse():
     ap.add_argument("--adjoint-n", type=int, default=512)
     ap.add_argument("--adjoint-steps", type=int, default=400)
     ap.add_argument("--adjoint-fd-dirs", type=int, default=64)
-    ap.add_argument("--adjoint-dual-dirs", type=int, default=2)
+    ap.add_argument("--adjoint-dual-dirs", type=int, default=1)
     return ap.parse_args()
 
 

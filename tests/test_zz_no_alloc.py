@@ -33,7 +33,7 @@ def _case(bottom: str):
     sc = S.circular_dam_break(96)
     from dataclasses import replace
     # a constant bottom of 0.1 that is not exact in Float32, with rain so the volume changes
-    return replace(sc, sources=[vf.ConstantRain(36.0)], eq={}, meta={"bottom_constant": 0.1})
+    return replace(sc, sources=[vf.SourceTermBottom(), vf.ConstantRain(36.0)], eq={}, meta={"bottom_constant": 0.1})
 
 
 def _build(sc, real):

@@ -107,6 +107,10 @@ void fill_geom(const vf_handle* h, vf::Geom<T>& g) {
   g.bc = h->cfg.bc;
 }
 
+// Float32 velocities with |h| below this many desingularizing_kappa are
+// divided in Float64.
+constexpr double VF_NEAR_DRY_FACTOR = 2.0;
+
 template <typename T>
 void fill_phys(const vf_handle* h, vf::Phys<T>& p) {
   const vf_config& c = h->cfg;
@@ -127,10 +131,14 @@ void fill_phys(const vf_handle* h, vf::Phys<T>& p) {
   p.dx_pow2 = std::frexp(dx, &ex) == 0.5 ? 1 : 0;
   p.dy_pow2 = std::frexp(dy, &ex) == 0.5 ? 1 : 0;
   p.Cz = (T)c.friction_Cz;
-  // Float32: velocities of cells and faces with |h| < 10 * depth_cutoff are
-  // divided in Float64 (VF_F32_NEAR_DRY=0 turns it off).
+  // Float32: velocities of cells and faces with |h| < VF_NEAR_DRY_FACTOR *
+  // desingularizing_kappa (the depth scale of the desingularised division,
+  // src/equations/equation.jl:40-67) are divided in Float64;
+  // VF_F32_NEAR_DRY=0 turns it off, VF_F32_NEAR_DRY_FACTOR overrides the factor.
   const char* nd = std::getenv("VF_F32_NEAR_DRY");
-  p.near_dry = (sizeof(T) == 4 && !(nd && std::strcmp(nd, "0") == 0)) ? (T)(10.0 * c.depth_cutoff) : (T)0;
+  const char* nf = std::getenv("VF_F32_NEAR_DRY_FACTOR");
+  const double factor = nf ? std::atof(nf) : VF_NEAR_DRY_FACTOR;
+  p.near_dry = (sizeof(T) == 4 && !(nd && std::strcmp(nd, "0") == 0)) ? (T)(factor * c.desingularizing_kappa) : (T)0;
   p.friction = c.friction;
   p.n_bottom = 0;
   p.n_point = 0;
