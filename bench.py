@@ -82,7 +82,6 @@ def parse():
     ap.add_argument("--adjoint-n", type=int, default=512)
     ap.add_argument("--adjoint-steps", type=int, default=400)
     ap.add_argument("--adjoint-fd-dirs", type=int, default=64)
-    ap.add_argument("--adjoint-dual-dirs", type=int, default=1)
     return ap.parse_args()
 
 
@@ -681,11 +680,12 @@ def adjoint_workload(n, steps):
 
 def measure_adjoint(args, local):
     """Gradient of the gauge loss by the GPU reverse sweep, checked against
-    central differences (smooth random directions) and the oracle on dual numbers."""
+    central differences on the device (smooth random directions). The checks
+    against the oracle on dual numbers and against extended-precision
+    differences run in the GPU tests."""
     import volumefluxes_sm103 as vf
     from volumefluxes_sm103 import adjoint as AD
     from volumefluxes_sm103 import scenarios as S
-    from oracle import vf_oracle as O
     case = S.differentiation_case(args.adjoint_n)
     sc, gauges, steps = case.scenario, case.gauges, args.adjoint_steps
     out = {"workload": adjoint_workload(args.adjoint_n, steps), "checkpoint_every": int(round(math.sqrt(steps)))}
@@ -717,7 +717,7 @@ def measure_adjoint(args, local):
     grid = sc.grid()
     f = vf.cell_faces(grid, interior=False)
     rng = np.random.default_rng(20241206)
-    rel, stable = [], []
+    rel = []
     for k in range(args.adjoint_fd_dirs):
         v = np.zeros_like(sc.B)
         for _ in range(3):
@@ -726,53 +726,20 @@ def measure_adjoint(args, local):
             v += rng.standard_normal() * np.exp(-((f[:, :, 0] - cx) ** 2 + (f[:, :, 1] - cy) ** 2) / (2 * s * s))
         vn = float(rng.standard_normal()) * 1e-3
         got = float(np.sum(gB * v)) + gCz * 2 * sc.manning_n * vn
-        fd = [AD.central_difference(sc, np.float64, gauges, target, dts, v, vn, e) for e in (FD_EPS, 4 * FD_EPS)]
-        rel.append(abs(fd[0] - got) / max(abs(got), 1e-300))
-        stable.append(AD.fd_consistent(fd[0], fd[1]))
-    rel, stable = np.array(rel), np.array(stable, dtype=bool)
+        fd = AD.central_difference(sc, np.float64, gauges, target, dts, v, vn, FD_EPS)
+        rel.append(abs(fd - got) / max(abs(got), 1e-300))
+    rel = np.array(rel)
     if len(rel):
         out["fd"] = {"directions": len(rel), "eps": FD_EPS, "rel_err_median": float(np.median(rel)),
                      "rel_err_p90": float(np.percentile(rel, 90)), "rel_err_max": float(rel.max()),
                      "within_1e-6": int((rel <= 1e-6).sum()),
-                     "fd_consistent": int(stable.sum()),
-                     "rel_err_max_consistent": float(rel[stable].max()) if stable.any() else None,
-                     "within_1e-6_consistent": int((rel[stable] <= 1e-6).sum()),
-                     "classification": "a direction is FD-consistent when its central differences at eps and "
-                                       "4*eps agree to 1e-7 relative; the others cross branch switches (minmod, "
-                                       "dry faces, the dry clamp) within the step, where the loss is not "
-                                       "differentiable and the difference quotient mixes one-sided slopes",
+                     "note": "Float64 central differences on the device: at this step some directions cross "
+                             "branch switches (minmod, dry faces, the dry clamp) and rounding of the gauge depths "
+                             "bounds the rest near 1e-7; the GPU tests compare the gradient with extended-precision "
+                             "differences on directions whose perturbed runs take the same branches (1e-6)",
                      "directions_kind": "sums of 3 random Gaussian bumps (width U[10,80] m) on B plus a random n "
                                         "component"}
-    # the oracle on dual numbers (the reference CPU path through ForwardDiff's stand-in)
-    if args.adjoint_dual_dirs > 0:
-        o = bench_oracle_sim(sc)
-        drel = []
-        t0 = time.perf_counter()
-        for k in range(args.adjoint_dual_dirs):
-            v = rng.standard_normal(sc.B.shape)
-            cz = float(rng.standard_normal()) * 1e-3
-            lo, dlo = O.dual_gauge_loss(o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target, Bdot=v, Cz_dot=cz)
-            got = float(np.sum(gB * v)) + gCz * cz
-            drel.append(abs(got - dlo) / abs(dlo))
-        out["dual_oracle"] = {"directions": len(drel), "rel_err_max": float(max(drel)),
-                              "loss_equal": bool(lo == loss), "seconds": time.perf_counter() - t0,
-                              "directions_kind": "white-noise B directions and a random Cz component"}
     return out
-
-
-def bench_oracle_sim(sc):
-    """The oracle built from a scenario (sources, friction) for the dual-number check."""
-    from oracle import vf_oracle as O
-    src = [(O.SRC_BOTTOM, 0.0)]
-    if sc.rain_m_per_h is not None:
-        src.append((O.SRC_CONST_RAIN, sc.rain_m_per_h))
-    if sc.infiltration_m_per_s is not None:
-        src.append((O.SRC_CONST_INFIL, sc.infiltration_m_per_s))
-    o = O.OracleSim(nx=sc.nx, ny=sc.ny, extent=sc.extent, real_bytes=8, theta=sc.theta, sources=src,
-                    friction=O.FRICTION_BSA2012, friction_Cz=sc.manning_n ** 2, stepper=O.STEPPER_RK2, cfl=sc.cfl,
-                    B=sc.B, **sc.eq)
-    o.set_interior(sc.w0, sc.hu0, sc.hv0)
-    return o
 
 
 def main():

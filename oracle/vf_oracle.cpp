@@ -29,6 +29,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <new>
 #include <vector>
 #ifdef _OPENMP
@@ -77,6 +78,10 @@ inline Dual vsqrt(Dual x) {
   const double r = std::sqrt(x.v);
   return Dual(r, r > 0 ? x.d / (2 * r) : 0.0);
 }
+inline bool vsignbit(long double x) { return std::signbit(x); }
+inline long double vabs(long double x) { return std::fabs(x); }
+inline long double vsqrt(long double x) { return std::sqrt(x); }
+inline long double vsign1(long double x) { return std::copysign(1.0L, x); }
 inline double vsign1(double x) { return std::copysign(1.0, x); }
 inline float vsign1(float x) { return std::copysign(1.0f, x); }
 inline Dual vsign1(Dual x) { return Dual(std::copysign(1.0, x.v), 0.0); }
@@ -91,6 +96,42 @@ template <typename T>
 inline T jl_min(T x, T y) {
   if (x != x || y != y) return x - y;
   return (x < y || (x == y && vsignbit(x))) ? x : y;
+}
+template <typename T>
+inline bool jl_max_picks_first(T x, T y) { return x > y || (x == y && !vsignbit(x)); }
+template <typename T>
+inline bool jl_min_picks_first(T x, T y) { return x < y || (x == y && vsignbit(x)); }
+
+// ---------------------------------------------------------------------------
+// Branch-outcome counters, test instrumentation for the gradient checks: when
+// switched on, every evaluation of a branch of the path (minmod case,
+// reconstruction clause, wet/dry face side, the kappa early-out and which
+// operand wins the wave-speed max/min, the desingularised depth, the dry
+// clamp) counts its outcome. Two runs whose counts agree took the same
+// branches everywhere (up to exact swaps between cells, which do not happen in
+// practice), so their loss difference is a smooth difference quotient; runs
+// whose counts differ crossed a kink. Off by default; the counting adds one
+// predictable test per branch.
+enum BranchId {
+  kBrMinmodMin, kBrMinmodMax, kBrMinmodZero, kBrRecLeft, kBrRecRight, kBrFaceMinusWet, kBrFacePlusWet, kBrFaceKappa,
+  kBrAplusP, kBrAplusM, kBrAplusZero, kBrAminusP, kBrAminusM, kBrAminusZero, kBrDesing, kBrClamp, kBrCount
+};
+struct BranchCounts {
+  uint64_t c[kBrCount];
+};
+bool g_branch_on = false;
+std::mutex g_branch_mu;
+std::vector<BranchCounts*> g_branch_all;  // one block per thread that counted
+thread_local BranchCounts* tl_branch = nullptr;
+inline void branch(int id) {
+  if (!g_branch_on) return;
+  if (!tl_branch) {
+    tl_branch = new BranchCounts();
+    std::memset(tl_branch->c, 0, sizeof(tl_branch->c));
+    std::lock_guard<std::mutex> lock(g_branch_mu);
+    g_branch_all.push_back(tl_branch);
+  }
+  ++tl_branch->c[id];
 }
 
 // ---------------------------------------------------------------------------
@@ -169,6 +210,9 @@ double cr_cbrt(double x) {
 }
 
 inline float cr_cbrt(float x) { return (float)cr_cbrt((double)x); }
+// Extended precision (the finite-difference reference of the gradient checks):
+// the library cube root, accurate to about one ulp of long double.
+inline long double cr_cbrt(long double x) { return std::cbrt(x); }
 inline Dual cr_cbrt(Dual x) {
   const double r = cr_cbrt(x.v);
   return Dual(r, x.v != 0 ? x.d * r / (3 * x.v) : 0.0);
@@ -265,6 +309,7 @@ struct Ops {
   T desing(T h) const {
     const T k = s.kappa;
     T m = jl_min<T>(h * h / ((T)2 * k) + k / (T)2.0, k);
+    if (g_branch_on && !jl_max_picks_first<T>(vabs(h), m)) branch(kBrDesing);
     return vsign1(h) * jl_max<T>(vabs(h), m);
   }
 
@@ -298,17 +343,27 @@ struct Ops {
   T central_upwind(const T* fminus, const T* fplus, int dir, T* F) const {
     T flm[3] = {0, 0, 0}, em[3] = {0, 0, 0};
     if (fminus[0] > s.cutoff) {
+      branch(kBrFaceMinusWet);
       phys_flux(dir, fminus, flm);
       eigen(dir, fminus, em);
     }
     T flp[3] = {0, 0, 0}, ep[3] = {0, 0, 0};
     if (fplus[0] > s.cutoff) {
+      branch(kBrFacePlusWet);
       phys_flux(dir, fplus, flp);
       eigen(dir, fplus, ep);
     }
     const T aplus = jl_max<T>(jl_max<T>(ep[0], em[0]), (T)0);
     const T aminus = jl_min<T>(jl_min<T>(ep[1], em[1]), (T)0);
+    if (g_branch_on) {
+      const T a1 = jl_max<T>(ep[0], em[0]), b1 = jl_min<T>(ep[1], em[1]);
+      branch(!jl_max_picks_first<T>(a1, (T)0) ? kBrAplusZero
+                                              : jl_max_picks_first<T>(ep[0], em[0]) ? kBrAplusP : kBrAplusM);
+      branch(!jl_min_picks_first<T>(b1, (T)0) ? kBrAminusZero
+                                              : jl_min_picks_first<T>(ep[1], em[1]) ? kBrAminusP : kBrAminusM);
+    }
     if (vabs(aplus - aminus) < s.kappa) {
+      branch(kBrFaceKappa);
       F[0] = F[1] = F[2] = 0;
       return 0;
     }
@@ -322,8 +377,15 @@ struct Ops {
 
   // --- src/reconstruction/linearreconstruction.jl:28-43 --------------------
   static T minmod(T a, T b, T c) {
-    if (a > 0 && b > 0 && c > 0) return jl_min<T>(jl_min<T>(a, b), c);
-    if (a < 0 && b < 0 && c < 0) return jl_max<T>(jl_max<T>(a, b), c);
+    if (a > 0 && b > 0 && c > 0) {
+      branch(kBrMinmodMin);
+      return jl_min<T>(jl_min<T>(a, b), c);
+    }
+    if (a < 0 && b < 0 && c < 0) {
+      branch(kBrMinmodMax);
+      return jl_max<T>(jl_max<T>(a, b), c);
+    }
+    branch(kBrMinmodZero);
     return 0;
   }
   static T minmod_slope(T l, T c, T r, T theta) {
@@ -379,8 +441,10 @@ struct Ops {
         const T B_right = Br(i, j, dir);
         const T w = at(Uin, 0, i, j);
         if (w - (T)0.5 * slope[0] < B_left) {
+          branch(kBrRecLeft);
           slope[0] = (T)2.0 * (w - B_left);
         } else if (w + (T)0.5 * slope[0] < B_right) {
+          branch(kBrRecRight);
           slope[0] = (T)2.0 * (B_right - w);
         }
         for (int k = 0; k < 3; ++k) {
@@ -540,6 +604,7 @@ struct Ops {
       for (int i = 0; i < s.N1; ++i) {
         const T b = Bc(i, j);
         if (at(out, 0, i, j) - b < s.cutoff) {
+          branch(kBrClamp);
           at(out, 0, i, j) = jl_max<T>(at(out, 0, i, j), b);
           at(out, 1, i, j) = 0;
           at(out, 2, i, j) = 0;
@@ -929,6 +994,32 @@ int vfo_update_bc_neumann(double* state, int nx, int ny, int gc) {
   return 0;
 }
 
+}  // extern "C"
+
+namespace {
+// From the given interior state, n_steps steps with the frozen dt sequence;
+// loss = sum over gauges of (w - target)^2 in the simulation's type.
+template <typename T>
+T frozen_gauge_loss(Sim<T>* s, const double* w, const double* hu, const double* hv, const double* dts, int n_steps,
+                    const int* gauge_i, const int* gauge_j, const double* target, int n_gauges) {
+  set_interior(s, w, hu, hv);
+  Ops<T> ops(*s);
+  for (int k = 0; k < n_steps; ++k) {
+    s->force_dt = dts[k];
+    ops.perform_step(std::numeric_limits<double>::infinity());
+  }
+  T L(0.0);
+  const int gc = s->p.gc;
+  for (int g = 0; g < n_gauges; ++g) {
+    const T x = s->U[0][s->id(gauge_i[g] + gc, gauge_j[g] + gc)] - T(target[g]);
+    L = L + x * x;
+  }
+  return L;
+}
+}  // namespace
+
+extern "C" {
+
 int vfo_dual_gauge_loss(const vfo_params* p, const double* B, const double* Bdot, double Cz_dot, const double* w,
                         const double* hu, const double* hv, const double* dts, int n_steps, const int* gauge_i,
                         const int* gauge_j, const double* target, int n_gauges, double* loss, double* dloss) {
@@ -939,22 +1030,59 @@ int vfo_dual_gauge_loss(const vfo_params* p, const double* B, const double* Bdot
   if (Bdot && !p->bottom_is_constant)
     for (size_t c = 0; c < s->B.size(); ++c) s->B[c].d = Bdot[c];
   s->Cz.d = Cz_dot;
-  set_interior(s, w, hu, hv);
-  Ops<Dual> ops(*s);
-  for (int k = 0; k < n_steps; ++k) {
-    s->force_dt = dts[k];
-    ops.perform_step(std::numeric_limits<double>::infinity());
-  }
-  Dual L(0.0);
-  const int gc = p->gc;
-  for (int g = 0; g < n_gauges; ++g) {
-    const Dual x = s->U[0][s->id(gauge_i[g] + gc, gauge_j[g] + gc)] - Dual(target[g]);
-    L = L + x * x;
-  }
+  const Dual L = frozen_gauge_loss<Dual>(s, w, hu, hv, dts, n_steps, gauge_i, gauge_j, target, n_gauges);
   *loss = L.v;
   if (dloss) *dloss = L.d;
   delete s;
   return 0;
+}
+
+int vfo_frozen_gauge_loss(const vfo_params* p, const double* B, const double* w, const double* hu, const double* hv,
+                          const double* dts, int n_steps, const int* gauge_i, const int* gauge_j,
+                          const double* target, int n_gauges, double* loss) {
+  if (check_params(p, B) || !loss || n_steps < 0 || (n_steps > 0 && !dts) || n_gauges < 0) return -1;
+  if (p->real_bytes != 8) return -1;
+  Sim<double>* s = make_sim<double>(p, B);
+  if (!s) return -2;
+  *loss = frozen_gauge_loss<double>(s, w, hu, hv, dts, n_steps, gauge_i, gauge_j, target, n_gauges);
+  delete s;
+  return 0;
+}
+
+int vfo_ext_gauge_loss(const vfo_params* p, const double* B, const double* Bdir, double Cz_dir1, double Cz_dir2,
+                       double eps, const double* w, const double* hu, const double* hv, const double* dts,
+                       int n_steps, const int* gauge_i, const int* gauge_j, const double* target, int n_gauges,
+                       double* loss_hi, double* loss_lo) {
+  if (check_params(p, B) || !loss_hi || !loss_lo || n_steps < 0 || (n_steps > 0 && !dts) || n_gauges < 0)
+    return -1;
+  if (p->real_bytes != 8) return -1;
+  Sim<long double>* s = make_sim<long double>(p, B);
+  if (!s) return -2;
+  const long double e = eps;
+  if (Bdir && !p->bottom_is_constant)
+    for (size_t c = 0; c < s->B.size(); ++c) s->B[c] = (long double)B[c] + e * (long double)Bdir[c];
+  s->Cz = (long double)p->friction_Cz + e * (long double)Cz_dir1 + e * e * (long double)Cz_dir2;
+  const long double L = frozen_gauge_loss<long double>(s, w, hu, hv, dts, n_steps, gauge_i, gauge_j, target, n_gauges);
+  *loss_hi = (double)L;
+  *loss_lo = (double)(L - (long double)*loss_hi);
+  delete s;
+  return 0;
+}
+
+void vfo_branch_counting(int on) {
+  std::lock_guard<std::mutex> lock(g_branch_mu);
+  for (BranchCounts* b : g_branch_all) std::memset(b->c, 0, sizeof(b->c));
+  g_branch_on = on != 0;
+}
+
+int vfo_branch_counts(unsigned long long* out, int n) {
+  std::lock_guard<std::mutex> lock(g_branch_mu);
+  for (int i = 0; i < n && i < kBrCount; ++i) {
+    unsigned long long sum = 0;
+    for (BranchCounts* b : g_branch_all) sum += b->c[i];
+    out[i] = sum;
+  }
+  return kBrCount;
 }
 
 double vfo_desingularize(double h, double kappa) {

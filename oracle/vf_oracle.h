@@ -112,6 +112,30 @@ int vfo_dual_gauge_loss(const vfo_params* p, const double* B, const double* Bdot
                         const double* hu, const double* hv, const double* dts, int n_steps, const int* gauge_i,
                         const int* gauge_j, const double* target, int n_gauges, double* loss, double* dloss);
 
+/* The same run in plain Float64 (the loss of vfo_dual_gauge_loss without a
+ * derivative). */
+int vfo_frozen_gauge_loss(const vfo_params* p, const double* B, const double* w, const double* hu, const double* hv,
+                          const double* dts, int n_steps, const int* gauge_i, const int* gauge_j,
+                          const double* target, int n_gauges, double* loss);
+
+/* The same run in extended precision (long double: 64-bit significand on
+ * x86, 113-bit on Arm), the reference of the gradient's finite-difference
+ * checks: bottom B + eps*Bdir and friction Cz + eps*Cz_dir1 + eps^2*Cz_dir2
+ * formed in that precision; the loss comes back as hi + lo. */
+int vfo_ext_gauge_loss(const vfo_params* p, const double* B, const double* Bdir, double Cz_dir1, double Cz_dir2,
+                       double eps, const double* w, const double* hu, const double* hv, const double* dts,
+                       int n_steps, const int* gauge_i, const int* gauge_j, const double* target, int n_gauges,
+                       double* loss_hi, double* loss_lo);
+
+/* Branch-outcome counters (instrumentation of the gradient checks): on != 0
+ * zeroes them and starts counting every branch outcome of the path (minmod
+ * case, reconstruction clause, wet face sides, the kappa early-out, the
+ * operand winning each wave-speed max/min, the desingularised depth, the dry
+ * clamp); on == 0 zeroes them and stops. vfo_branch_counts writes up to n
+ * counters and returns how many exist. */
+void vfo_branch_counting(int on);
+int vfo_branch_counts(unsigned long long* out, int n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -78,6 +78,12 @@ def load():
         "vfo_desingularize": (D, [D, D]),
         "vfo_dual_gauge_loss": (C.c_int, [C.POINTER(Params), P, P, D, P, P, P, P, C.c_int, P, P, P, C.c_int,
                                           C.POINTER(D), C.POINTER(D)]),
+        "vfo_frozen_gauge_loss": (C.c_int, [C.POINTER(Params), P, P, P, P, P, C.c_int, P, P, P, C.c_int,
+                                            C.POINTER(D)]),
+        "vfo_ext_gauge_loss": (C.c_int, [C.POINTER(Params), P, P, D, D, D, P, P, P, P, C.c_int, P, P, P, C.c_int,
+                                         C.POINTER(D), C.POINTER(D)]),
+        "vfo_branch_counting": (None, [C.c_int]),
+        "vfo_branch_counts": (C.c_int, [C.POINTER(C.c_ulonglong), C.c_int]),
     }
     for n, (r, a) in sig.items():
         f = getattr(lib, n)
@@ -226,3 +232,74 @@ def dual_gauge_loss(sim: OracleSim, w, hu, hv, dts, gauges, target, *, B=None, B
 
 def get_threads() -> int:
     return load().vfo_get_threads()
+
+
+def _gauge_args(sim, w, hu, hv, dts, gauges, target, B, Cz):
+    p = Params()
+    C.pointer(p)[0] = sim.p
+    if Cz is not None:
+        p.friction_Cz = float(Cz)
+    Bt = sim._B if B is None else np.ascontiguousarray(np.asarray(B, dtype=np.float64).T)
+    arrs = [np.ascontiguousarray(np.asarray(a, dtype=np.float64).T) for a in (w, hu, hv)]
+    d = np.ascontiguousarray(dts, dtype=np.float64)
+    g = np.asarray(gauges, dtype=np.int32)
+    gi, gj = np.ascontiguousarray(g[:, 0]), np.ascontiguousarray(g[:, 1])
+    tg = np.ascontiguousarray(target, dtype=np.float64)
+    return p, Bt, arrs, d, gi, gj, tg
+
+
+def frozen_gauge_loss(sim: OracleSim, w, hu, hv, dts, gauges, target, *, B=None, Cz=None) -> float:
+    """The loss of dual_gauge_loss in plain Float64: from the interior state,
+    len(dts) steps with the frozen dt sequence, B / Cz overriding sim's."""
+    p, Bt, arrs, d, gi, gj, tg = _gauge_args(sim, w, hu, hv, dts, gauges, target, B, Cz)
+    loss = C.c_double()
+    rc = sim.lib.vfo_frozen_gauge_loss(C.byref(p), _p(Bt), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), _p(d), len(d),
+                                       _p(gi), _p(gj), _p(tg), len(tg), C.byref(loss))
+    if rc != 0:
+        raise ValueError(f"oracle frozen run failed ({rc})")
+    return loss.value
+
+
+def branch_signature(run) -> tuple:
+    """Branch-outcome counts of the oracle while `run()` executes (see
+    vfo_branch_counting): runs with equal signatures took the same branches."""
+    lib = load()
+    lib.vfo_branch_counting(1)
+    try:
+        run()
+        out = (C.c_ulonglong * 32)()
+        n = lib.vfo_branch_counts(out, 32)
+        return tuple(int(out[i]) for i in range(n))
+    finally:
+        lib.vfo_branch_counting(0)
+
+
+def ext_gauge_loss(sim: OracleSim, w, hu, hv, dts, gauges, target, *, Bdir=None, Cz_dir1=0.0, Cz_dir2=0.0,
+                   eps=0.0):
+    """The frozen-dt loss in extended precision (long double) at B + eps*Bdir and
+    Cz + eps*Cz_dir1 + eps^2*Cz_dir2 (perturbations formed in that precision),
+    as (hi, lo) doubles whose sum is the loss."""
+    p, Bt, arrs, d, gi, gj, tg = _gauge_args(sim, w, hu, hv, dts, gauges, target, None, None)
+    Bd = None if Bdir is None else np.ascontiguousarray(np.asarray(Bdir, dtype=np.float64).T)
+    hi, lo = C.c_double(), C.c_double()
+    rc = sim.lib.vfo_ext_gauge_loss(C.byref(p), _p(Bt), None if Bd is None else _p(Bd), float(Cz_dir1),
+                                    float(Cz_dir2), float(eps), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), _p(d), len(d),
+                                    _p(gi), _p(gj), _p(tg), len(tg), C.byref(hi), C.byref(lo))
+    if rc != 0:
+        raise ValueError(f"oracle extended-precision run failed ({rc})")
+    return hi.value, lo.value
+
+
+def ext_central_difference(sim: OracleSim, w, hu, hv, dts, gauges, target, Bdir, Cz_dir1, Cz_dir2, eps):
+    """Central difference of the loss along (Bdir, Cz) in extended precision,
+    with the branch-outcome signatures of the +eps and -eps runs:
+    (fd, sig_plus, sig_minus)."""
+    runs = {}
+    sigs = {}
+    for sign in (1, -1):
+        def run(sign=sign):
+            runs[sign] = ext_gauge_loss(sim, w, hu, hv, dts, gauges, target, Bdir=Bdir, Cz_dir1=Cz_dir1,
+                                        Cz_dir2=Cz_dir2, eps=sign * eps)
+        sigs[sign] = branch_signature(run)
+    (ph, pl), (mh, ml) = runs[1], runs[-1]
+    return ((ph - mh) + (pl - ml)) / (2 * eps), sigs[1], sigs[-1]

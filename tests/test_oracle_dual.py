@@ -59,3 +59,48 @@ def test_dual_derivative_matches_central_differences():
     lm, _ = O.dual_gauge_loss(o.o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target, Cz=cz - eps)
     fd = (lp - lm) / (2 * eps)
     assert abs(fd - dcz) <= 1e-3 * max(abs(dcz), 1e-12), (fd, dcz)
+
+
+def test_frozen_run_and_branch_signature():
+    """The plain frozen-dt run gives the dual run's value bit for bit; its
+    branch-outcome signature is reproducible, and a large perturbation of the
+    bottom changes it (a branch switch is detected)."""
+    sc, o, dts, gauges, target, _ = _case()
+    lo, _ = O.dual_gauge_loss(o.o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target)
+    assert O.frozen_gauge_loss(o.o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target) == lo
+
+    def run(B=None):
+        return lambda: O.frozen_gauge_loss(o.o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target, B=B)
+
+    a, b = O.branch_signature(run()), O.branch_signature(run())
+    assert a == b and sum(a) > 0
+    rng = np.random.default_rng(3)
+    assert O.branch_signature(run(sc.B + 0.05 * rng.standard_normal(sc.B.shape))) != a
+
+
+def test_extended_precision_differences_match_the_dual_derivative():
+    """Central differences in extended precision with a step small enough to
+    stay on one branch (checked with the branch signatures) agree with the
+    dual-number derivative to 1e-6: the derivative the oracle and the device
+    adjoint follow is the derivative of the loss where the loss is smooth."""
+    sc, o, dts, gauges, target, _ = _case()
+    hi, lo = O.ext_gauge_loss(o.o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target)
+    plain = O.frozen_gauge_loss(o.o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target)
+    assert abs((hi + lo) - plain) <= 1e-10 * abs(plain)
+    base = O.branch_signature(lambda: O.frozen_gauge_loss(o.o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target))
+    rng = np.random.default_rng(5)
+    x = np.arange(sc.B.shape[0])[:, None]
+    y = np.arange(sc.B.shape[1])[None, :]
+    n0 = math.sqrt(o.p.friction_Cz)
+    stable = 0
+    for k in range(6):
+        cx, cy, s = rng.uniform(4, 20), rng.uniform(4, 20), rng.uniform(3, 8)
+        v = np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2 * s * s))
+        vn = float(rng.standard_normal()) * 1e-3
+        fd, sp, sm = O.ext_central_difference(o.o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target, v, 2 * n0 * vn,
+                                              vn * vn, 1e-9)
+        _, d = O.dual_gauge_loss(o.o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target, Bdot=v, Cz_dot=2 * n0 * vn)
+        if sp == base and sm == base:
+            stable += 1
+            assert abs(fd - d) <= 1e-6 * abs(d), (k, fd, d)
+    assert stable >= 5

@@ -144,9 +144,6 @@ except ImportError:  # torch is optional for the library itself
     GaugeLoss = None
 
 
-FD_CONSISTENCY = 1e-7
-
-
 def central_difference(sc, real, gauges, target, dts, Bdir, n_dir: float, eps: float) -> float:
     """(loss(B + eps*Bdir, n + eps*n_dir) - loss(B - eps*Bdir, n - eps*n_dir)) / (2 eps),
     each loss a forward run on the device with the frozen dt sequence."""
@@ -155,10 +152,3 @@ def central_difference(sc, real, gauges, target, dts, Bdir, n_dir: float, eps: f
     lm = gauge_loss(sc, real, gauges, target, dts, B=sc.B - eps * Bdir, manning_n=n0 - eps * n_dir)
     return (lp - lm) / (2 * eps)
 
-
-def fd_consistent(fd_eps: float, fd_4eps: float, tol: float = FD_CONSISTENCY) -> bool:
-    """Whether central differences at eps and 4*eps agree to `tol` relative: on a
-    path whose branches (minmod cases, dry faces, the dry clamp) stay fixed over
-    the perturbation the loss is smooth and the two agree to truncation and
-    rounding error; a branch switch inside the step makes them differ."""
-    return abs(fd_eps - fd_4eps) <= tol * max(abs(fd_eps), abs(fd_4eps))
