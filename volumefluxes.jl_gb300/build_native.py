@@ -3,8 +3,10 @@
 Eight translation units compile in parallel with nvcc and link into one shared
 library with the CUDA runtime linked statically:
 
-  vf_f64.cu  Float64 kernels, -fmad=false (each operation rounds as in Julia);
-             tile kernels held to 80 registers (three resident blocks per SM)
+  vf_f64.cu  Float64 kernels, -fmad=false (each operation rounds as in Julia),
+             quotients through correctly rounded reciprocals (VF_FP64_MARKSTEIN:
+             the IEEE quotient's bits); tile kernels held to 80 registers
+             (three resident blocks per SM)
   vf_f64f.cu Float64 per-step kernels with faithful quotients, -fmad=true
              (VF_ARITH_FAITHFUL; held to a tolerance, not to the bits)
   vf_f32.cu  Float32 kernels, contraction and fast division allowed
@@ -35,7 +37,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-strict-aliasing",
           f"-I{INCLUDE}", f"-I{CSRC}"]
 UNITS = {
-    "vf_f64.cu": ["-fmad=false", "-DVF_TILE_MIN_BLOCKS=3"],
+    "vf_f64.cu": ["-fmad=false", "-DVF_TILE_MIN_BLOCKS=3", "-DVF_FP64_MARKSTEIN=1"],
     "vf_f64f.cu": ["-fmad=true", "-DVF_TILE_MIN_BLOCKS=3"],
     "vf_f32.cu": ["-fmad=true", "-ftz=true", "-prec-sqrt=false"],
     "vf_abi.cu": [],
