@@ -806,7 +806,7 @@ def main():
             }
             if dt == "f64" and mode == "reference":
                 r["compute_roofline"] = fp64_roofline(sc, m["dev_stage"], (m["clocks"] or {}).get("sm_mhz"), fp64_inst)
-        if args.steps < FULL_STEPS:
+        if args.steps < FULL_STEPS and args.start_steps == 0 and not args.state_in:
             r["window_note"] = (f"{args.steps} steps from the initial state: the flow starts at rest (no friction work "
                                 f"for the first ~15 steps), so this window runs faster per step than the "
                                 f"configuration's {FULL_STEPS} steps; see full_config")
