@@ -201,6 +201,13 @@ int vf_time_kernels(vf_handle* h, int64_t n_steps, float* ms_flux, float* ms_sta
  * returns either way. No reference counterpart (failure-detection test hook). */
 int vf_selftest_tile_wait(int32_t device, int32_t arrive, int32_t iterations, int32_t* gave_up);
 
+/* Self-test of the Float64 quotient every Float64 kernel uses (correctly
+ * rounded reciprocals shared by a divisor's quotients, with the IEEE division
+ * for the operands the method excludes): q[i] = a[i] / b[i] for n host
+ * pairs, computed on the device. It must equal IEEE division bit for bit. No
+ * reference counterpart (test hook). */
+int vf_selftest_quotients(int32_t device, const double* a, const double* b, int32_t n, double* q);
+
 /* ---- Batched ensemble ------------------------------------------------------
  * Advances many independent simulations, each a handle set up as above, each
  * to its own end time with its own CFL dt: the loop of simulate_to_time

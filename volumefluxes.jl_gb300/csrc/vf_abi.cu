@@ -776,6 +776,22 @@ int vf_selftest_tile_wait(int32_t device, int32_t arrive, int32_t iterations, in
   return VF_OK;
 }
 
+int vf_selftest_quotients(int32_t device, const double* a, const double* b, int32_t n, double* q) {
+  if (!a || !b || !q || n < 1) return fail(nullptr, VF_EINVAL, "a, b, q must be non-NULL and n >= 1");
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+  double* d = nullptr;
+  const size_t bytes = sizeof(double) * (size_t)n;
+  if ((e = cudaMalloc(&d, 3 * bytes)) != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
+  e = cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = vf::launch_selftest_quotients(d, d + n, n, d + 2 * (size_t)n, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(q, d + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "quotient self-test");
+  return VF_OK;
+}
+
 int vf_time_steps(vf_handle* h, int64_t n_steps, float* ms_out) {
   int rc = ensure_ready(h);
   if (rc) return rc;

@@ -49,6 +49,17 @@ cudaError_t launch_sample(const Geom<double>& g, const double* U, const int* ij,
   k_sample<double><<<(n + 127) / 128, 128, 0, st>>>(g, U, ij, n, out);
   return cudaGetLastError();
 }
+// The Float64 quotient of every kernel of this unit (a / b through Arith<double>::recip
+// and div_by), element by element: the self-test of vf_selftest_quotients.
+static __global__ void k_selftest_quotients(const double* a, const double* b, int n, double* q) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) q[i] = Arith<double>::div_by(Arith<double>::recip(b[i]), a[i]);
+}
+cudaError_t launch_selftest_quotients(const double* a, const double* b, int n, double* q, cudaStream_t st) {
+  k_selftest_quotients<<<(n + 255) / 256, 256, 0, st>>>(a, b, n, q);
+  return cudaGetLastError();
+}
+
 cudaError_t configure_kernels_f64() {
   const cudaError_t e = configure_impl<double>();
   return e != cudaSuccess ? e : vf_faithful_configure();

@@ -118,8 +118,10 @@ struct Arith<double> {
   //     in one fused multiply-add, and RN(q0 + (a - b*q0)*y) is RN(a/b).
   // The steps need normal operands with quotients far from overflow and
   // underflow: a divisor with an all-ones significand or an exponent outside
-  // +-500, or a nonzero numerator outside that range, takes the IEEE division.
-  // A zero numerator returns a*y, the correctly signed zero.
+  // +-500 (zero, subnormal, infinite and NaN divisors included), or a nonzero
+  // numerator outside that range (infinite and NaN numerators included),
+  // takes the IEEE division. A zero numerator over an in-range divisor
+  // returns a*y, the correctly signed zero.
   struct Recip {
     double b, y;
     bool ok;
@@ -138,9 +140,10 @@ struct Arith<double> {
     return Recip{b, fma(y1, e1, y1), mid_range(bb) && (bb & 0xfffffffffffffll) != 0xfffffffffffffll};
   }
   static __device__ __forceinline__ double div_by(const Recip& R, double a) {
+    if (!R.ok) return a / R.b;
     const double q0 = a * R.y;
     if (is_zero(a)) return q0;
-    if (!R.ok || !mid_range(bits(a))) return a / R.b;
+    if (!mid_range(bits(a))) return a / R.b;
     return fma(fma(-R.b, q0, a), R.y, q0);
   }
   static __device__ __forceinline__ double div(double a, double b) { return div_by(recip(b), a); }
