@@ -997,16 +997,34 @@ int vfo_update_bc_neumann(double* state, int nx, int ny, int gc) {
 }  // extern "C"
 
 namespace {
-// From the given interior state, n_steps steps with the frozen dt sequence;
+// The source tables and per-cell source fields of an existing Float64
+// simulation (TimeDependentRain, HortonInfiltration, a rain field), converted
+// to the real type of dst.
+template <typename T>
+void copy_sources(Sim<T>* dst, const vfo_sim* like) {
+  if (!like) return;
+  const Handle* h = reinterpret_cast<const Handle*>(like);
+  if (!h->d) return;
+  for (int i = 0; i < VFO_MAX_SOURCES; ++i) {
+    dst->src_times[i] = h->d->src_times[i];
+    dst->src_rates[i] = h->d->src_rates[i];
+    dst->src_field[i].assign(h->d->src_field[i].begin(), h->d->src_field[i].end());
+  }
+}
+
+// From the given interior state at t = 0, n_steps steps with the frozen dt
+// sequence, t += dt after each (the time of the time-dependent sources);
 // loss = sum over gauges of (w - target)^2 in the simulation's type.
 template <typename T>
 T frozen_gauge_loss(Sim<T>* s, const double* w, const double* hu, const double* hv, const double* dts, int n_steps,
                     const int* gauge_i, const int* gauge_j, const double* target, int n_gauges) {
   set_interior(s, w, hu, hv);
   Ops<T> ops(*s);
+  s->t = 0.0;
   for (int k = 0; k < n_steps; ++k) {
     s->force_dt = dts[k];
     ops.perform_step(std::numeric_limits<double>::infinity());
+    s->t = s->t + dts[k];
   }
   T L(0.0);
   const int gc = s->p.gc;
@@ -1022,11 +1040,13 @@ extern "C" {
 
 int vfo_dual_gauge_loss(const vfo_params* p, const double* B, const double* Bdot, double Cz_dot, const double* w,
                         const double* hu, const double* hv, const double* dts, int n_steps, const int* gauge_i,
-                        const int* gauge_j, const double* target, int n_gauges, double* loss, double* dloss) {
+                        const int* gauge_j, const double* target, int n_gauges, double* loss, double* dloss,
+                        const vfo_sim* like) {
   if (check_params(p, B) || !loss || n_steps < 0 || (n_steps > 0 && !dts) || n_gauges < 0) return -1;
   if (p->real_bytes != 8) return -1;
   Sim<Dual>* s = make_sim<Dual>(p, B);
   if (!s) return -2;
+  copy_sources(s, like);
   if (Bdot && !p->bottom_is_constant)
     for (size_t c = 0; c < s->B.size(); ++c) s->B[c].d = Bdot[c];
   s->Cz.d = Cz_dot;
@@ -1039,11 +1059,12 @@ int vfo_dual_gauge_loss(const vfo_params* p, const double* B, const double* Bdot
 
 int vfo_frozen_gauge_loss(const vfo_params* p, const double* B, const double* w, const double* hu, const double* hv,
                           const double* dts, int n_steps, const int* gauge_i, const int* gauge_j,
-                          const double* target, int n_gauges, double* loss) {
+                          const double* target, int n_gauges, double* loss, const vfo_sim* like) {
   if (check_params(p, B) || !loss || n_steps < 0 || (n_steps > 0 && !dts) || n_gauges < 0) return -1;
   if (p->real_bytes != 8) return -1;
   Sim<double>* s = make_sim<double>(p, B);
   if (!s) return -2;
+  copy_sources(s, like);
   *loss = frozen_gauge_loss<double>(s, w, hu, hv, dts, n_steps, gauge_i, gauge_j, target, n_gauges);
   delete s;
   return 0;
@@ -1052,12 +1073,13 @@ int vfo_frozen_gauge_loss(const vfo_params* p, const double* B, const double* w,
 int vfo_ext_gauge_loss(const vfo_params* p, const double* B, const double* Bdir, double Cz_dir1, double Cz_dir2,
                        double eps, const double* w, const double* hu, const double* hv, const double* dts,
                        int n_steps, const int* gauge_i, const int* gauge_j, const double* target, int n_gauges,
-                       double* loss_hi, double* loss_lo) {
+                       double* loss_hi, double* loss_lo, const vfo_sim* like) {
   if (check_params(p, B) || !loss_hi || !loss_lo || n_steps < 0 || (n_steps > 0 && !dts) || n_gauges < 0)
     return -1;
   if (p->real_bytes != 8) return -1;
   Sim<long double>* s = make_sim<long double>(p, B);
   if (!s) return -2;
+  copy_sources(s, like);
   const long double e = eps;
   if (Bdir && !p->bottom_is_constant)
     for (size_t c = 0; c < s->B.size(); ++c) s->B[c] = (long double)B[c] + e * (long double)Bdir[c];

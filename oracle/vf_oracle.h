@@ -104,19 +104,21 @@ double vfo_cbrt(double x);
 double vfo_desingularize(double h, double kappa);
 
 /* Float64 dual-number run (the stand-in for ForwardDiff through this path):
- * from the given interior state, n_steps steps with the frozen dt sequence
- * dts, bottom corners B + eps*Bdot (Bdot may be NULL) and friction Cz +
- * eps*Cz_dot; returns loss = sum over gauges of (w[i,j] - target)^2 (interior
- * 0-based indices) and d loss / d eps. */
+ * from the given interior state at t = 0, n_steps steps with the frozen dt
+ * sequence dts (t += dt after each), bottom corners B + eps*Bdot (Bdot may be
+ * NULL) and friction Cz + eps*Cz_dot; returns loss = sum over gauges of
+ * (w[i,j] - target)^2 (interior 0-based indices) and d loss / d eps. `like`
+ * (may be NULL) lends its source tables and per-cell source fields. */
 int vfo_dual_gauge_loss(const vfo_params* p, const double* B, const double* Bdot, double Cz_dot, const double* w,
                         const double* hu, const double* hv, const double* dts, int n_steps, const int* gauge_i,
-                        const int* gauge_j, const double* target, int n_gauges, double* loss, double* dloss);
+                        const int* gauge_j, const double* target, int n_gauges, double* loss, double* dloss,
+                        const vfo_sim* like);
 
 /* The same run in plain Float64 (the loss of vfo_dual_gauge_loss without a
  * derivative). */
 int vfo_frozen_gauge_loss(const vfo_params* p, const double* B, const double* w, const double* hu, const double* hv,
                           const double* dts, int n_steps, const int* gauge_i, const int* gauge_j,
-                          const double* target, int n_gauges, double* loss);
+                          const double* target, int n_gauges, double* loss, const vfo_sim* like);
 
 /* The same run in extended precision (long double: 64-bit significand on
  * x86, 113-bit on Arm), the reference of the gradient's finite-difference
@@ -125,7 +127,7 @@ int vfo_frozen_gauge_loss(const vfo_params* p, const double* B, const double* w,
 int vfo_ext_gauge_loss(const vfo_params* p, const double* B, const double* Bdir, double Cz_dir1, double Cz_dir2,
                        double eps, const double* w, const double* hu, const double* hv, const double* dts,
                        int n_steps, const int* gauge_i, const int* gauge_j, const double* target, int n_gauges,
-                       double* loss_hi, double* loss_lo);
+                       double* loss_hi, double* loss_lo, const vfo_sim* like);
 
 /* Branch-outcome counters (instrumentation of the gradient checks): on != 0
  * zeroes them and starts counting every branch outcome of the path (minmod

@@ -77,11 +77,11 @@ def load():
         "vfo_update_bc_neumann": (C.c_int, [P, C.c_int, C.c_int, C.c_int]),
         "vfo_desingularize": (D, [D, D]),
         "vfo_dual_gauge_loss": (C.c_int, [C.POINTER(Params), P, P, D, P, P, P, P, C.c_int, P, P, P, C.c_int,
-                                          C.POINTER(D), C.POINTER(D)]),
+                                          C.POINTER(D), C.POINTER(D), P]),
         "vfo_frozen_gauge_loss": (C.c_int, [C.POINTER(Params), P, P, P, P, P, C.c_int, P, P, P, C.c_int,
-                                            C.POINTER(D)]),
+                                            C.POINTER(D), P]),
         "vfo_ext_gauge_loss": (C.c_int, [C.POINTER(Params), P, P, D, D, D, P, P, P, P, C.c_int, P, P, P, C.c_int,
-                                         C.POINTER(D), C.POINTER(D)]),
+                                         C.POINTER(D), C.POINTER(D), P]),
         "vfo_branch_counting": (None, [C.c_int]),
         "vfo_branch_counts": (C.c_int, [C.POINTER(C.c_ulonglong), C.c_int]),
     }
@@ -224,7 +224,7 @@ def dual_gauge_loss(sim: OracleSim, w, hu, hv, dts, gauges, target, *, B=None, B
     loss, dloss = C.c_double(), C.c_double()
     rc = lib.vfo_dual_gauge_loss(C.byref(p), _p(Bt), None if Bd is None else _p(Bd), float(Cz_dot), _p(arrs[0]),
                                  _p(arrs[1]), _p(arrs[2]), _p(d), len(d), _p(gi), _p(gj), _p(tg), len(tg),
-                                 C.byref(loss), C.byref(dloss))
+                                 C.byref(loss), C.byref(dloss), sim.h)
     if rc != 0:
         raise ValueError(f"oracle dual run failed ({rc})")
     return loss.value, dloss.value
@@ -254,7 +254,7 @@ def frozen_gauge_loss(sim: OracleSim, w, hu, hv, dts, gauges, target, *, B=None,
     p, Bt, arrs, d, gi, gj, tg = _gauge_args(sim, w, hu, hv, dts, gauges, target, B, Cz)
     loss = C.c_double()
     rc = sim.lib.vfo_frozen_gauge_loss(C.byref(p), _p(Bt), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), _p(d), len(d),
-                                       _p(gi), _p(gj), _p(tg), len(tg), C.byref(loss))
+                                       _p(gi), _p(gj), _p(tg), len(tg), C.byref(loss), sim.h)
     if rc != 0:
         raise ValueError(f"oracle frozen run failed ({rc})")
     return loss.value
@@ -284,7 +284,7 @@ def ext_gauge_loss(sim: OracleSim, w, hu, hv, dts, gauges, target, *, Bdir=None,
     hi, lo = C.c_double(), C.c_double()
     rc = sim.lib.vfo_ext_gauge_loss(C.byref(p), _p(Bt), None if Bd is None else _p(Bd), float(Cz_dir1),
                                     float(Cz_dir2), float(eps), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), _p(d), len(d),
-                                    _p(gi), _p(gj), _p(tg), len(tg), C.byref(hi), C.byref(lo))
+                                    _p(gi), _p(gj), _p(tg), len(tg), C.byref(hi), C.byref(lo), sim.h)
     if rc != 0:
         raise ValueError(f"oracle extended-precision run failed ({rc})")
     return hi.value, lo.value

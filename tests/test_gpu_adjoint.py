@@ -150,3 +150,62 @@ def test_autograd_function_gives_the_adjoint_gradient():
     assert float(L.detach()) == loss
     assert np.array_equal(B.grad.numpy(), gB)
     assert float(n.grad) == gCz * 2 * case.scenario.manning_n
+
+
+def _variant(kind):
+    """The small differentiation case under forward Euler, PeriodicBC, or with
+    TimeDependentRain and HortonInfiltration (a seeded per-cell factor)."""
+    from dataclasses import replace
+    case, gauges, steps = small_case(n=40, steps=20)
+    sc = case.scenario
+    if kind == "fe":
+        sc = replace(sc, stepper="fe")
+    elif kind == "periodic":
+        sc = replace(sc, bc="periodic")
+    elif kind == "fe_periodic":
+        sc = replace(sc, stepper="fe", bc="periodic")
+    elif kind == "dynamic_sources":
+        grid = sc.grid()
+        rng = np.random.default_rng(3)
+        factor = rng.uniform(0.5, 1.5, (sc.nx + 4, sc.ny + 4))
+        sc = replace(sc, sources=[vf.SourceTermBottom(),
+                                  vf.TimeDependentRain(np.array([200.0, 20.0, 300.0]), np.array([0.0, 2.0, 4.0])),
+                                  vf.HortonInfiltration(grid, vf.SM103Backend(), factor=factor, f0=4e-3, fc=1e-4,
+                                                        k=0.5)])
+    return replace(case, scenario=sc), gauges, steps
+
+
+@pytest.mark.parametrize("kind", ["fe", "periodic", "fe_periodic", "dynamic_sources"])
+def test_adjoint_beyond_the_differentiation_workload(kind):
+    """Forward Euler, PeriodicBC and the time-dependent sources against the
+    dual-number oracle (the ForwardDiff stand-in): the forward pass is the
+    oracle's bit for bit and the gradient agrees to 1e-9."""
+    case, gauges, steps = _variant(kind)
+    sc = case.scenario
+    dts, target, loss, gB, gCz = run_adjoint(case, gauges, steps)
+    o = oracle_from(sc)
+    ref = []
+    for _ in range(steps):
+        dt = o.perform_step(math.inf)
+        o.o.t = o.o.t + dt  # the adjoint's forward pass runs from t = 0 with t += dt
+        ref.append(dt)
+    assert list(dts) == ref
+    o = oracle_from(sc)
+    rng = np.random.default_rng(13)
+    for k in range(3):
+        v = rng.standard_normal(sc.B.shape)
+        cz = float(rng.standard_normal()) * 1e-3
+        lo, dlo = O.dual_gauge_loss(o.o, sc.w0, sc.hu0, sc.hv0, dts, gauges, target, Bdot=v, Cz_dot=cz)
+        assert lo == loss
+        got = float(np.sum(gB * v)) + gCz * cz
+        assert abs(got - dlo) <= 1e-9 * abs(dlo), (k, got, dlo)
+
+
+def test_adjoint_rejects_what_it_does_not_cover():
+    from dataclasses import replace
+    case, gauges, steps = small_case(n=24, steps=4)
+    for sc in (replace(case.scenario, reconstruction="none"), replace(case.scenario, bc="neumann")):
+        sim = sc.build(vf.SM103Backend(np.float64))
+        with pytest.raises(vf.ArgumentError):
+            AD.GaugeAdjoint(sim, steps)
+        sim.close()

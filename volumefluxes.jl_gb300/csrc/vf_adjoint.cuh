@@ -482,14 +482,22 @@ __global__ void __launch_bounds__(256) k_adj_gather(AdjArgs<T> a) {
   T lam[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) lam[k] = a.lam_direct[k * g.PS + o] + land(0, x, y, k) + land(1, x, y, k);
-  // ghosts mirroring this cell: x ghosts at x' = 2gc-1-x (left) or 2(gc+nx)-1-x (right)
+  // ghosts copying this cell: wall ghosts mirror it, x' = 2gc-1-x (left) or
+  // 2(gc+nx)-1-x (right), with the normal momentum negated; periodic ghosts
+  // repeat it a period away, x' = x + n (right) or x - n (left)
+  // (src/bc.jl:29-40, 81-110)
 #pragma unroll
   for (int dir = 0; dir < 2; ++dir) {
     const int v = dir == 0 ? x : y;
     const int n = dir == 0 ? g.nx : g.ny;
     int gh[2] = {-1, -1};
-    if (v < 2 * g.gc) gh[0] = 2 * g.gc - 1 - v;                  // left/bottom ghost
-    if (v >= g.gc + n - g.gc) gh[1] = 2 * (g.gc + n) - 1 - v;    // right/top ghost
+    if (g.bc == 2) {
+      if (v - n >= 0 && v - n < g.gc) gh[0] = v - n;            // left/bottom ghost
+      if (v + n >= g.gc + n && v + n < 2 * g.gc + n) gh[1] = v + n;  // right/top ghost
+    } else {
+      if (v < 2 * g.gc) gh[0] = 2 * g.gc - 1 - v;                  // left/bottom ghost
+      if (v >= g.gc + n - g.gc) gh[1] = 2 * (g.gc + n) - 1 - v;    // right/top ghost
+    }
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
       const int q = gh[s];
@@ -498,7 +506,7 @@ __global__ void __launch_bounds__(256) k_adj_gather(AdjArgs<T> a) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const T l = land(dir, gx, gy, k);
-        const bool normal = (dir == 0 && k == 1) || (dir == 1 && k == 2);
+        const bool normal = g.bc == 1 && ((dir == 0 && k == 1) || (dir == 1 && k == 2));
         lam[k] = lam[k] + (normal ? -l : l);
       }
     }

@@ -48,6 +48,7 @@ struct vf_adjoint {
   vf::StepRecord* rec = nullptr;
   vf::StepRecord rec_h;
   std::vector<double> dts;
+  std::vector<double> ts;  // start time of every step of the forward pass (time-dependent sources)
   bool have_forward = false;
   std::string err;
 };
@@ -97,9 +98,10 @@ vf::StepArgs<double>& args_of<double>(vf_handle* h) { return h->ad; }
 template <>
 vf::StepArgs<float>& args_of<float>(vf_handle* h) { return h->af; }
 
-int set_dt(vf_adjoint* a, double dt) {
+int set_dt(vf_adjoint* a, double dt, double t) {
   std::memset(&a->rec_h, 0, sizeof(a->rec_h));
   a->rec_h.active[0] = 1;
+  a->rec_h.t[0] = t;
   a->rec_h.explicit_mode = 1;
   a->rec_h.force_dt = 1;
   a->rec_h.forced_dt = dt;
@@ -111,9 +113,9 @@ int set_dt(vf_adjoint* a, double dt) {
 
 // One forward step of the checkpointed recomputation: Uin -> Uout with dt.
 template <typename T>
-int fwd_step(vf_adjoint* a, const void* Uin, void* Uout, double dt) {
+int fwd_step(vf_adjoint* a, const void* Uin, void* Uout, double dt, double t) {
   vf_handle* h = a->h;
-  if (int rc = set_dt(a, dt)) return rc;
+  if (int rc = set_dt(a, dt, t)) return rc;
   vf::StepArgs<T> s = args_of<T>(h);
   s.L = static_cast<T*>(a->L0);
   s.S = static_cast<T*>(a->S0);
@@ -162,26 +164,39 @@ int reverse_stage(vf_adjoint* a, vf::AdjArgs<T> x) {
   return VF_OK;
 }
 
-// Reverse of step n whose input state is U0: lam holds lambda of U^{n+1} on
-// entry and lambda of U^n on return.
+// Reverse of step n whose input state is U0 (start time t): lam holds lambda of
+// U^{n+1} on entry and lambda of U^n on return. Forward Euler is the RK2 first
+// stage alone (src/timestepper/forwardeuler.jl:28-47): its output is U^{n+1}.
 template <typename T>
-int reverse_step(vf_adjoint* a, const void* U0, double dt) {
+int reverse_step(vf_adjoint* a, const void* U0, double dt, double t) {
   vf_handle* h = a->h;
-  if (int rc = set_dt(a, dt)) return rc;
+  if (int rc = set_dt(a, dt, t)) return rc;
   vf::StepArgs<T> s = args_of<T>(h);
   s.rec = a->rec;
   s.arith = VF_ARITH_REFERENCE;
-  // recompute L(U0), S(U0), U1, L(U1), S(U1)
+  // recompute L(U0), S(U0) (and for RK2 U1, L(U1), S(U1))
   s.L = static_cast<T*>(a->L0);
   s.S = static_cast<T*>(a->S0);
   VF_ACK(a, vf::launch_flux(s, static_cast<const T*>(U0), 0, h->stream));
+  h->launches += 1;
+  if (!s.rk2) {
+    vf::AdjArgs<T> x1 = adj_args<T>(a, dt);
+    x1.stage2 = 0;
+    x1.Uprev = static_cast<const T*>(U0);
+    x1.L = static_cast<const T*>(a->L0);
+    x1.lam_out = static_cast<const T*>(a->lam);
+    x1.lam_in = static_cast<T*>(a->lamU1);
+    if (int rc = reverse_stage<T>(a, x1)) return rc;
+    std::swap(a->lam, a->lamU1);  // lambda of U^n now in lam
+    return VF_OK;
+  }
   vf::StepArgs<T> fe = s;
   fe.rk2 = 0;
   VF_ACK(a, vf::launch_stage(fe, static_cast<const T*>(U0), static_cast<T*>(a->U1), 0, h->stream));
   s.L = static_cast<T*>(a->L1);
   s.S = static_cast<T*>(a->S1);
   VF_ACK(a, vf::launch_flux(s, static_cast<const T*>(a->U1), 0, h->stream));
-  h->launches += 3;
+  h->launches += 2;
   // stage 2
   vf::AdjArgs<T> x2 = adj_args<T>(a, dt);
   x2.stage2 = 1;
@@ -238,10 +253,11 @@ int backward_impl(vf_adjoint* a, const int32_t* gi, const int32_t* gj, const dou
                               cudaMemcpyDeviceToDevice, st));
     for (int n = start; n + 1 < end; ++n)
       if (int rc = fwd_step<T>(a, off(a->seg, (size_t)(n - start) * a->state_bytes),
-                               off(a->seg, (size_t)(n - start + 1) * a->state_bytes), a->dts[n]))
+                               off(a->seg, (size_t)(n - start + 1) * a->state_bytes), a->dts[n], a->ts[n]))
         return rc;
     for (int n = end - 1; n >= start; --n)
-      if (int rc = reverse_step<T>(a, off(a->seg, (size_t)(n - start) * a->state_bytes), a->dts[n])) return rc;
+      if (int rc = reverse_step<T>(a, off(a->seg, (size_t)(n - start) * a->state_bytes), a->dts[n], a->ts[n]))
+        return rc;
   }
   double gcz = 0, loss = 0;
   VF_ACK(a, cudaMemcpyAsync(&gcz, a->gCz, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -265,17 +281,21 @@ int vf_adjoint_create(vf_handle* h, int32_t n_steps, int32_t checkpoint_every, v
   if (!h || n_steps < 1) return afail(nullptr, VF_EINVAL, "need a handle and n_steps >= 1");
   if (int rc = vf::handle_ready(h)) return afail(nullptr, rc, std::string("handle not ready: ") + h->err);
   const vf_config& c = h->cfg;
-  if (c.stepper != VF_STEPPER_RK2 || c.reconstruction != VF_REC_LINEAR || c.bc != VF_BC_WALL ||
-      c.bottom_is_constant)
+  if ((c.stepper != VF_STEPPER_RK2 && c.stepper != VF_STEPPER_FE) || c.reconstruction != VF_REC_LINEAR ||
+      (c.bc != VF_BC_WALL && c.bc != VF_BC_PERIODIC) || c.bottom_is_constant)
     return afail(nullptr, VF_EINVAL,
-                 "the adjoint covers RungeKutta2, LinearReconstruction, WallBC and a BottomTopography2D");
+                 "the adjoint covers RungeKutta2 and ForwardEulerStepper, LinearReconstruction, WallBC and PeriodicBC, "
+                 "and a BottomTopography2D");
   if (c.friction != VF_FRICTION_NONE && c.friction != VF_FRICTION_BSA2012 && c.friction != VF_FRICTION_FCG2016 &&
       c.friction != VF_FRICTION_BH2021)
     return afail(nullptr, VF_EINVAL, "unknown friction law");
   for (int i = 0; i < c.n_sources; ++i)
     if (c.source_kind[i] != VF_SRC_BOTTOM && c.source_kind[i] != VF_SRC_CONST_RAIN &&
-        c.source_kind[i] != VF_SRC_CONST_INFIL)
-      return afail(nullptr, VF_EINVAL, "the adjoint covers SourceTermBottom, ConstantRain and ConstantInfiltration");
+        c.source_kind[i] != VF_SRC_CONST_INFIL && c.source_kind[i] != VF_SRC_TIME_RAIN &&
+        c.source_kind[i] != VF_SRC_HORTON)
+      return afail(nullptr, VF_EINVAL,
+                   "the adjoint covers SourceTermBottom, ConstantRain, ConstantInfiltration, TimeDependentRain and "
+                   "HortonInfiltration (a FunctionalRain field changes on the host between steps)");
   vf_adjoint* a = new (std::nothrow) vf_adjoint();
   if (!a) return afail(nullptr, VF_ENOMEM, "host allocation failed");
   a->h = h;
@@ -318,8 +338,10 @@ int vf_adjoint_forward(vf_adjoint* a, const double* frozen_dts, double* dts_out)
   VF_ACK(a, cudaSetDevice(h->device));
   VF_ACK(a, cudaMemcpyAsync(h->U[0], a->init, a->state_bytes, cudaMemcpyDeviceToDevice, h->stream));
   a->dts.assign(a->n_steps, 0.0);
+  a->ts.assign(a->n_steps, 0.0);
   double t = 0.0;
   for (int n = 0; n < a->n_steps; ++n) {
+    a->ts[n] = t;
     if (n % a->K == 0)
       VF_ACK(a, cudaMemcpyAsync(off(a->ckpt, (size_t)(n / a->K) * a->state_bytes), h->U[0], a->state_bytes,
                                 cudaMemcpyDeviceToDevice, h->stream));
