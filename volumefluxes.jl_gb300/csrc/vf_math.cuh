@@ -17,15 +17,12 @@
 #include <cuda_runtime.h>
 
 
-// Float32 reciprocals and cube roots from the special-function unit (1:
-// rcp.approx, and cbrt(x) = 2^(log2|x| / 3) with the sign of x; a few ulps) or
-// the correctly rounded reciprocal and the libm cube root (0). Float32 results
-// are stated against the Float64 oracle, not claimed bitwise. Measured on the
-// 4096^2 wet/dry step (Float32 is instruction-issue bound): 0.919 ms with the
-// special-function unit, 1.069 ms without.
-#ifndef VF_F32_FAST_SFU
-#define VF_F32_FAST_SFU 1
-#endif
+// Float32 reciprocals and cube roots come from the special-function unit
+// (rcp.approx, and cbrt(x) = 2^(log2|x| / 3) with the sign of x; a few ulps);
+// Float32 results are stated against the Float64 oracle, not claimed bitwise.
+// Measured on the 4096^2 wet/dry step (Float32 is instruction-issue bound):
+// 0.919 ms with the special-function unit, 1.069 ms with the correctly
+// rounded reciprocal and the libm cube root.
 // Float64 quotients correct to about one ulp instead of correctly rounded (1),
 // for the tolerance-bound Float64 kernels (vf_f64f.cu, built with multiply-add
 // contraction): a reciprocal from the hardware approximation refined by one
@@ -178,11 +175,7 @@ struct Arith<float> {
   static __device__ __forceinline__ float max(float x, float y) { return fmaxf(x, y); }
   static __device__ __forceinline__ float min(float x, float y) { return fminf(x, y); }
   static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
-#if VF_F32_FAST_SFU
   static __device__ __forceinline__ float rcp(float b) { return __fdividef(1.0f, b); }
-#else
-  static __device__ __forceinline__ float rcp(float b) { return __frcp_rn(b); }
-#endif
   static __device__ __forceinline__ float sqrt_(float x) { return sqrtf(x); }
   // Quotients over one divisor: one reciprocal, then products.
   struct Recip {
@@ -266,15 +259,11 @@ template <> __device__ __forceinline__ double vcbrt<double>(double x) { return c
 #else
 template <> __device__ __forceinline__ double vcbrt<double>(double x) { return cr_cbrt(x); }
 #endif
-#if VF_F32_FAST_SFU
 template <> __device__ __forceinline__ float vcbrt<float>(float x) {
   float y;
   asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(__log2f(fabsf(x)) * (1.0f / 3.0f)));
   return copysignf(y, x);
 }
-#else
-template <> __device__ __forceinline__ float vcbrt<float>(float x) { return cbrtf(x); }
-#endif
 
 // Back-compat names used by the tile kernels.
 template <typename T> __device__ __forceinline__ T jmax(T x, T y) { return Arith<T>::max(x, y); }
