@@ -320,10 +320,10 @@ const char* vf_server_last_error(vf_server* s);
  * (test/test_swe_ad.jl, examples/optimization.jl); these calls replace that
  * for large parameter counts: one reverse sweep gives dLoss/dB for every
  * bottom corner and dLoss/dCz at once. Covered: RungeKutta2 and
- * ForwardEulerStepper, LinearReconstruction, WallBC and PeriodicBC, a
- * BottomTopography2D, SourceTermBottom, ConstantRain, ConstantInfiltration,
- * TimeDependentRain, HortonInfiltration and any ImplicitFriction law (not
- * NoReconstruction, NeumannBC or FunctionalRain, whose field the host
+ * ForwardEulerStepper, LinearReconstruction and NoReconstruction, WallBC and
+ * PeriodicBC, a BottomTopography2D, SourceTermBottom, ConstantRain,
+ * ConstantInfiltration, TimeDependentRain, HortonInfiltration and any
+ * ImplicitFriction law (not NeumannBC, or FunctionalRain, whose field the host
  * re-evaluates between steps). The run's time starts at 0. At kinks
  * (minmod switches, dry faces, the dry clamp) the gradient is the
  * derivative of the branch the forward pass took. */

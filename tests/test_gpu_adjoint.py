@@ -153,8 +153,9 @@ def test_autograd_function_gives_the_adjoint_gradient():
 
 
 def _variant(kind):
-    """The small differentiation case under forward Euler, PeriodicBC, or with
-    TimeDependentRain and HortonInfiltration (a seeded per-cell factor)."""
+    """The small differentiation case under forward Euler, PeriodicBC,
+    NoReconstruction, or with TimeDependentRain and HortonInfiltration (a
+    seeded per-cell factor)."""
     from dataclasses import replace
     case, gauges, steps = small_case(n=40, steps=20)
     sc = case.scenario
@@ -164,6 +165,10 @@ def _variant(kind):
         sc = replace(sc, bc="periodic")
     elif kind == "fe_periodic":
         sc = replace(sc, stepper="fe", bc="periodic")
+    elif kind == "no_reconstruction":
+        sc = replace(sc, reconstruction="none")
+    elif kind == "no_reconstruction_fe_periodic":
+        sc = replace(sc, reconstruction="none", stepper="fe", bc="periodic")
     elif kind == "dynamic_sources":
         grid = sc.grid()
         rng = np.random.default_rng(3)
@@ -175,9 +180,10 @@ def _variant(kind):
     return replace(case, scenario=sc), gauges, steps
 
 
-@pytest.mark.parametrize("kind", ["fe", "periodic", "fe_periodic", "dynamic_sources"])
+@pytest.mark.parametrize("kind", ["fe", "periodic", "fe_periodic", "dynamic_sources", "no_reconstruction",
+                                  "no_reconstruction_fe_periodic"])
 def test_adjoint_beyond_the_differentiation_workload(kind):
-    """Forward Euler, PeriodicBC and the time-dependent sources against the
+    """Forward Euler, PeriodicBC, NoReconstruction and the time-dependent sources against the
     dual-number oracle (the ForwardDiff stand-in): the forward pass is the
     oracle's bit for bit and the gradient agrees to 1e-9."""
     case, gauges, steps = _variant(kind)
@@ -204,7 +210,7 @@ def test_adjoint_beyond_the_differentiation_workload(kind):
 def test_adjoint_rejects_what_it_does_not_cover():
     from dataclasses import replace
     case, gauges, steps = small_case(n=24, steps=4)
-    for sc in (replace(case.scenario, reconstruction="none"), replace(case.scenario, bc="neumann")):
+    for sc in (replace(case.scenario, bc="neumann"),):
         sim = sc.build(vf.SM103Backend(np.float64))
         with pytest.raises(vf.ArgumentError):
             AD.GaugeAdjoint(sim, steps)

@@ -346,6 +346,13 @@ __global__ void __launch_bounds__(128) k_adj_recon(AdjArgs<T> a) {
     }
     return right ? (T)0.5 * (a.B[b + g.PB] + a.B[b + g.PB + 1]) : (T)0.5 * (a.B[b] + a.B[b + 1]);
   };
+  // B_cell of the cell at offset s along DIR, in the forward kernels' order
+  // (NoReconstruction's face depth is w - B_cell, src/reconstruction/noreconstruction.jl:30-46)
+  auto bcell = [&](int s) -> T {
+    if (g.bottom_const) return g.bconst;
+    const long long b = (long long)Y(s) * g.PB + X(s) + XOFF;
+    return (T)0.25 * (((a.B[b] + a.B[b + 1]) + a.B[b + g.PB]) + a.B[b + g.PB + 1]);
+  };
   const T inv = DIR == 0 ? p.inv_dx : p.inv_dy;
   // Stencil values at offsets -2..+2 (only what is used is read).
   T u[5][3];
@@ -358,14 +365,21 @@ __global__ void __launch_bounds__(128) k_adj_recon(AdjArgs<T> a) {
   // reconstruction of cells c-1, c, c+1 (forward)
   T Lc[3], Rc[3], Rm[3], Lp[3];
   const T Blc = bface(0, 0), Brc = bface(0, 1);
-  reconstruct_cell<T>(p, u[1], u[2], u[3], Blc, Brc, Lc, Rc);
-  if (face_l) {
-    T Lm[3];
-    reconstruct_cell<T>(p, u[0], u[1], u[2], bface(-1, 0), bface(-1, 1), Lm, Rm);
-  }
-  if (face_r) {
-    T Rp[3];
-    reconstruct_cell<T>(p, u[2], u[3], u[4], bface(1, 0), bface(1, 1), Lp, Rp);
+  if (p.rec_none) {
+    no_reconstruction<T>(u[2], bcell(0), Lc, Rc);
+    T tmp[3];
+    if (face_l) no_reconstruction<T>(u[1], bcell(-1), tmp, Rm);
+    if (face_r) no_reconstruction<T>(u[3], bcell(1), Lp, tmp);
+  } else {
+    reconstruct_cell<T>(p, u[1], u[2], u[3], Blc, Brc, Lc, Rc);
+    if (face_l) {
+      T Lm[3];
+      reconstruct_cell<T>(p, u[0], u[1], u[2], bface(-1, 0), bface(-1, 1), Lm, Rm);
+    }
+    if (face_r) {
+      T Rp[3];
+      reconstruct_cell<T>(p, u[2], u[3], u[4], bface(1, 0), bface(1, 1), Lp, Rp);
+    }
   }
   T lR[3] = {0, 0, 0}, lL[3] = {0, 0, 0};
   const Phys<Dual<T>> dp = dual_phys(p);
@@ -416,13 +430,24 @@ __global__ void __launch_bounds__(128) k_adj_recon(AdjArgs<T> a) {
   }
   // reconstruction of cell c in reverse
   T lu[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // [neighbour -1, 0, +1][component]
+  if (p.rec_none) {
+    // L = R = (w - B_cell, hu, hv): the cell takes both faces' lambda, and
+    // d/dB_cell = -(lambda_L.h + lambda_R.h) goes to the corners a quarter
+    // each, i.e. half to each face bottom of this direction (whose corners
+    // are the cell's, a half each)
 #pragma unroll
-  for (int k = 1; k < 3; ++k) {  // hu, hv: L = c - s/2, R = c + s/2
+    for (int k = 0; k < 3; ++k) lu[1][k] = lL[k] + lR[k];
+    const T dBc = (T)0 - (lL[0] + lR[0]);
+    gBl = gBl + (T)0.5 * dBc;
+    gBr = gBr + (T)0.5 * dBc;
+  }
+#pragma unroll
+  for (int k = 1; k < 3 && !p.rec_none; ++k) {  // hu, hv: L = c - s/2, R = c + s/2
     lu[1][k] = lu[1][k] + lL[k] + lR[k];
     const T ls = (T)0.5 * (lR[k] - lL[k]);
     minmod_slope_rev<T>(u[1][k], u[2][k], u[3][k], p.theta, ls, lu[0][k], lu[1][k], lu[2][k]);
   }
-  {  // w with the bottom-limited slope
+  if (!p.rec_none) {  // w with the bottom-limited slope
     const T w = u[2][0];
     const T s0 = minmod_slope<T>(u[1][0], u[2][0], u[3][0], p.theta);
     // L0 = (w - s/2) - Bl, R0 = (w + s/2) - Br

@@ -281,11 +281,12 @@ int vf_adjoint_create(vf_handle* h, int32_t n_steps, int32_t checkpoint_every, v
   if (!h || n_steps < 1) return afail(nullptr, VF_EINVAL, "need a handle and n_steps >= 1");
   if (int rc = vf::handle_ready(h)) return afail(nullptr, rc, std::string("handle not ready: ") + h->err);
   const vf_config& c = h->cfg;
-  if ((c.stepper != VF_STEPPER_RK2 && c.stepper != VF_STEPPER_FE) || c.reconstruction != VF_REC_LINEAR ||
+  if ((c.stepper != VF_STEPPER_RK2 && c.stepper != VF_STEPPER_FE) ||
+      (c.reconstruction != VF_REC_LINEAR && c.reconstruction != VF_REC_NONE) ||
       (c.bc != VF_BC_WALL && c.bc != VF_BC_PERIODIC) || c.bottom_is_constant)
     return afail(nullptr, VF_EINVAL,
-                 "the adjoint covers RungeKutta2 and ForwardEulerStepper, LinearReconstruction, WallBC and PeriodicBC, "
-                 "and a BottomTopography2D");
+                 "the adjoint covers RungeKutta2 and ForwardEulerStepper, LinearReconstruction and NoReconstruction, "
+                 "WallBC and PeriodicBC, and a BottomTopography2D");
   if (c.friction != VF_FRICTION_NONE && c.friction != VF_FRICTION_BSA2012 && c.friction != VF_FRICTION_FCG2016 &&
       c.friction != VF_FRICTION_BH2021)
     return afail(nullptr, VF_EINVAL, "unknown friction law");
