@@ -794,7 +794,8 @@ def main():
         if mode == "faithful":
             r["arithmetic"] = "faithful quotients and fused multiply-adds (VF_ARITH_FAITHFUL)"
         if dt == "f32":
-            r["near_dry_f64_division"] = mode != "no_near_dry"
+            r["near_dry_division"] = ("the Float64 quotient's bits (correctly rounded Float32 division) where "
+                                      "|h| < 2 kappa" if mode != "no_near_dry" else "fast reciprocal everywhere")
         if "full_ms" in m:
             full_ms = m["full_ms"]
             r["full_config"] = {

@@ -208,6 +208,15 @@ int vf_selftest_tile_wait(int32_t device, int32_t arrive, int32_t iterations, in
  * reference counterpart (test hook). */
 int vf_selftest_quotients(int32_t device, const double* a, const double* b, int32_t n, double* q);
 
+/* Self-test of the near-dry velocity quotient of the Float32 kernels (face
+ * sides and cells with |h| below the near-dry threshold divide (hu, hv) by
+ * the desingularised depth this way): q[i] as the kernels compute a[i] / b[i],
+ * and q64[i] = the IEEE Float64 quotient rounded to Float32, both on the
+ * device for n host pairs. The two must be equal bit for bit wherever the
+ * operands and the quotient are normal Float32 numbers (the Float32 kernels
+ * flush subnormals to zero). No reference counterpart (test hook). */
+int vf_selftest_near_dry_quotients(int32_t device, const float* a, const float* b, int32_t n, float* q, float* q64);
+
 /* ---- Batched ensemble ------------------------------------------------------
  * Advances many independent simulations, each a handle set up as above, each
  * to its own end time with its own CFL dt: the loop of simulate_to_time

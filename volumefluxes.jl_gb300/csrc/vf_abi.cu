@@ -792,6 +792,24 @@ int vf_selftest_quotients(int32_t device, const double* a, const double* b, int3
   return VF_OK;
 }
 
+int vf_selftest_near_dry_quotients(int32_t device, const float* a, const float* b, int32_t n, float* q,
+                                   float* q64) {
+  if (!a || !b || !q || !q64 || n < 1) return fail(nullptr, VF_EINVAL, "a, b, q, q64 must be non-NULL and n >= 1");
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+  float* d = nullptr;
+  const size_t bytes = sizeof(float) * (size_t)n;
+  if ((e = cudaMalloc(&d, 4 * bytes)) != cudaSuccess) return cuda_fail(nullptr, e, "cudaMalloc");
+  e = cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = vf::launch_selftest_near_dry(d, d + n, n, d + 2 * (size_t)n, d + 3 * (size_t)n, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(q, d + 2 * (size_t)n, bytes, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(q64, d + 3 * (size_t)n, bytes, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(nullptr, e, "near-dry quotient self-test");
+  return VF_OK;
+}
+
 int vf_time_steps(vf_handle* h, int64_t n_steps, float* ms_out) {
   int rc = ensure_ready(h);
   if (rc) return rc;

@@ -40,5 +40,19 @@ cudaError_t launch_sample(const Geom<float>& g, const float* U, const int* ij, i
   k_sample<float><<<(n + 127) / 128, 128, 0, st>>>(g, U, ij, n, out);
   return cudaGetLastError();
 }
+// The near-dry velocity quotient as the Float32 kernels compute it (q) and the
+// IEEE Float64 quotient rounded to Float32 (q64), element by element: the
+// self-test of vf_selftest_near_dry_quotients.
+static __global__ void k_selftest_near_dry(const float* a, const float* b, int n, float* q, float* q64) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    q[i] = f64_quotient_f32(a[i], b[i]);
+    q64[i] = (float)((double)a[i] / (double)b[i]);
+  }
+}
+cudaError_t launch_selftest_near_dry(const float* a, const float* b, int n, float* q, float* q64, cudaStream_t st) {
+  k_selftest_near_dry<<<(n + 255) / 256, 256, 0, st>>>(a, b, n, q, q64);
+  return cudaGetLastError();
+}
 cudaError_t configure_kernels_f32() { return configure_impl<float>(); }
 }  // namespace vf

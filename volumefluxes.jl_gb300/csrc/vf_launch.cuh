@@ -76,6 +76,7 @@ cudaError_t launch_adj_seed(const Geom<float>& g, const float* U, float* lam, co
 cudaError_t launch_adj_sum(const double* part, int n, double* acc, cudaStream_t st);
 // Float64 quotients a[i] / b[i] as the Float64 kernels compute them (self-test).
 cudaError_t launch_selftest_quotients(const double* a, const double* b, int n, double* q, cudaStream_t st);
+cudaError_t launch_selftest_near_dry(const float* a, const float* b, int n, float* q, float* q64, cudaStream_t st);
 // Opt the big-shared-memory kernels in on the current device (idempotent).
 cudaError_t configure_kernels_f64();
 cudaError_t configure_kernels_f32();

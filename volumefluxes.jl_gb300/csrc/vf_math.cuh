@@ -387,29 +387,29 @@ __device__ __forceinline__ T desing(T h, T kappa) {
   return copysign((T)1, h) * A::max(fabs(h), m);
 }
 
+// The Float64 quotient a/b of two Float32 values, rounded to Float32, without
+// Float64 instructions. Rounding an IEEE quotient to 53 bits and then to 24
+// gives the same bits as rounding it to 24 bits once, because 53 >= 2*24
+// (Figueroa, "When is double rounding innocuous?", SIGNUM Newsl. 30(3), 1995),
+// so RN32(RN64(a/b)) is the correctly rounded Float32 quotient, which
+// __fdiv_rn computes on the Float32 pipes whatever the -prec-div setting. The
+// kernels divide near-dry velocities with it: GB300 runs Float64 at 1/64 of
+// the Float32 rate, so the Float64 instructions cost a divergent warp several
+// hundred cycles per quotient. vf_selftest_near_dry_quotients checks the
+// equality against the IEEE Float64 division on the device.
+__device__ __forceinline__ float f64_quotient_f32(float a, float b) { return __fdiv_rn(a, b); }
+
 // Desingularised velocities (hu, hv) / h* (src/equations/equation.jl:40-67).
-// A Float32 state divides in Float64 where |h| < p.near_dry (the thin films
-// at wet/dry fronts; out of line, so the common path keeps its registers) and
-// with one fast reciprocal elsewhere; Float64 and dual numbers divide in their
-// own type. The Float64 reciprocal is the hardware approximation refined by
-// one third-order Newton step (about one Float64 ulp), far below the Float32
-// rounding of the result.
-static __device__ __noinline__ float2 velocity_f64(float hs, float hu, float hv) {
-  const double b = (double)hs;
-  double r0;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r0) : "d"(b));
-  const double e = fma(-b, r0, 1.0);
-  const double r = fma(r0, fma(e, e, e), r0);
-  return make_float2((float)((double)hu * r), (float)((double)hv * r));
-}
+// A Float32 state takes the Float64 quotient (f64_quotient_f32) where
+// |h| < p.near_dry, the thin films at wet/dry fronts, and one fast reciprocal
+// elsewhere; Float64 and dual numbers divide in their own type.
 template <typename T>
 __device__ __forceinline__ void velocities(const Phys<T>& p, T h, T hs, T hu, T hv, T& u, T& v) {
   using A = Arith<T>;
   if constexpr (sizeof(T) == 4) {
     if (A::abs_lt(h, p.near_dry)) {
-      const float2 uv = velocity_f64(hs, hu, hv);
-      u = uv.x;
-      v = uv.y;
+      u = f64_quotient_f32(hu, hs);
+      v = f64_quotient_f32(hv, hs);
       return;
     }
   }

@@ -30,6 +30,7 @@ EXPORTED_SYMBOLS = (
     "vf_set_interior_state", "vf_upload_state",
     "vf_download_state", "vf_get_interior_state", "vf_step", "vf_set_arithmetic", "vf_simulate", "vf_water_volume",
     "vf_device_state", "vf_stream", "vf_time_steps", "vf_time_kernels", "vf_selftest_tile_wait", "vf_selftest_quotients",
+    "vf_selftest_near_dry_quotients",
     "vf_last_error",
     "vf_launch_count",
     "vf_water_volume_static",
@@ -122,6 +123,8 @@ def load(build_if_missing: bool = False):
         "vf_time_steps": (C.c_int, [H, C.c_int64, C.POINTER(C.c_float)]),
         "vf_selftest_tile_wait": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
         "vf_selftest_quotients": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+        "vf_selftest_near_dry_quotients": (C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p,
+                                                     C.c_void_p]),
         "vf_time_kernels": (C.c_int, [H, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "vf_last_error": (C.c_char_p, [H]),
         "vf_water_volume_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
