@@ -182,6 +182,10 @@ void fill_phys(const vf_handle* h, vf::Phys<T>& p) {
       p.any_dynamic = 1;
     }
   }
+  double sum = 0.0;
+  for (int n = 0; n < p.n_point; ++n) sum += (double)p.point_add[n];
+  p.point_sum = (T)sum;
+  p.bottom_g = (T)(p.n_bottom * -c.g);
 }
 
 // cuTensorMapEncodeTiled from the driver, looked up once through the runtime

@@ -17,6 +17,7 @@
 //            the RK2 average, friction, dry clamp and U2's wall ghosts
 //            (src/timestepper/rungekutta.jl:26-52, src/simulator.jl:145-177).
 #pragma once
+#include <type_traits>
 #include "vf_kernels.cuh"
 
 namespace vf {
@@ -24,6 +25,12 @@ namespace vf {
 constexpr int MW = 32;        // lanes per strip
 constexpr int MOUT = 28;      // output columns per strip
 constexpr int MWPB = 4;       // warps (strips) per block
+// Desingularisation without a branch (desing<T, true>) in the Float32 flux
+// pass, with the branch in the stage pass: at 4096^2 the flux pass measured
+// 0.334 instead of 0.343 ms with it; the stage pass, held to 64 registers,
+// spills more with it and measured 0.485 instead of 0.475 ms. Same bits.
+constexpr bool kFluxSel = true;
+constexpr bool kStageSel = false;
 
 template <typename T>
 __device__ __forceinline__ T shfl_up1(T v) { return __shfl_up_sync(0xffffffffu, v, 1); }
@@ -37,6 +44,7 @@ struct StripGeom {
   int ys, ye;          // output rows [ys, ye)
   bool out_col;        // lane holds an output column inside the domain
   bool ld_col;         // column inside the stored array
+  bool xedge;          // some lane of the strip is a ghost column or one of the two columns next to one
 };
 
 // Strip `strip`, row segment `seg` (of seg_rows rows) for the calling warp.
@@ -51,6 +59,9 @@ __device__ __forceinline__ bool strip_setup_at(const Geom<T>& g, int seg_rows, i
   s.ye = min(s.ys + seg_rows, g.gc + g.ny);
   s.out_col = s.lane >= 2 && s.lane < 2 + MOUT && s.x < g.gc + g.nx;
   s.ld_col = s.x < g.N1;
+  // Lanes span columns xs-2 .. xs+29; ghost columns are < gc and >= gc+nx,
+  // and the two interior columns beside each side write wall ghosts.
+  s.xedge = s.xs - 2 <= g.gc + 1 || s.xs + (MW - 3) >= g.gc + g.nx - 2;
   return true;
 }
 
@@ -125,18 +136,32 @@ __device__ __forceinline__ void recon(const Phys<T>& p, const Cell3<T>& l, const
   R = Cell3<T>{Rv[0], Rv[1], Rv[2]};
 }
 
-template <typename T, int DIR, bool SPEED>
+template <typename T, int DIR, bool SPEED, bool SEL>
 __device__ __forceinline__ Cell3<T> face(const Phys<T>& p, const Cell3<T>& m, const Cell3<T>& q, T& speed) {
   Cell3<T> F;
-  cu_face<T, DIR, SPEED>(p, m.w, m.hu, m.hv, q.w, q.hu, q.hv, F.w, F.hu, F.hv, speed);
+  cu_face<T, DIR, SPEED, SEL>(p, m.w, m.hu, m.hv, q.w, q.hu, q.hv, F.w, F.hu, F.hv, speed);
   return F;
+}
+
+// Bottom source of one direction added to acc (src/sourceterms/source_term_bottom.jl:34-40):
+// once per SourceTermBottom entry in order; Float32 adds n_bottom * (-g) times
+// the term at once (no loop; the same value for the usual single entry up to
+// where multiply-add contraction falls).
+template <typename T>
+__device__ __forceinline__ T add_bottom(const Phys<T>& p, T acc, T slope, T hmean) {
+  if constexpr (sizeof(T) == 4) {
+    return acc + p.bottom_g * slope * hmean;
+  } else {
+    for (int b = 0; b < p.n_bottom; ++b) acc = acc + p.neg_g * slope * hmean;
+    return acc;
+  }
 }
 
 // x-direction contribution of row j for this lane: -(1/Δx)(F_{x+1/2} - F_{x-1/2})
 // plus the bottom source along x (src/numericalflux/numericalflux.jl:24-30,
 // src/sourceterms/source_term_bottom.jl:34-40). Every lane participates in the
 // shuffles; lanes 2..30 compute valid faces x-1/2.
-template <typename T, bool SPEED>
+template <typename T, bool SPEED, bool SEL>
 __device__ __forceinline__ Cell3<T> x_derivative(const Geom<T>& g, const Phys<T>& p, const Cell3<T>& u,
                                                  const CornerRow<T>& clo, const CornerRow<T>& chi, T& sx) {
   Cell3<T> ul{shfl_up1(u.w), shfl_up1(u.hu), shfl_up1(u.hv)};
@@ -147,15 +172,14 @@ __device__ __forceinline__ Cell3<T> x_derivative(const Geom<T>& g, const Phys<T>
   recon<T>(p, ul, u, ur, bl, br, L, R);
   const Cell3<T> Rm{shfl_up1(R.w), shfl_up1(R.hu), shfl_up1(R.hv)};
   T sp = (T)0;
-  const Cell3<T> Fl = face<T, 0, SPEED>(p, Rm, L, sp);  // face x-1/2
+  const Cell3<T> Fl = face<T, 0, SPEED, SEL>(p, Rm, L, sp);  // face x-1/2
   if (SPEED) sx = sp;
   const Cell3<T> Fr{shfl_dn1(Fl.w), shfl_dn1(Fl.hu), shfl_dn1(Fl.hv)};
   Cell3<T> acc;
   acc.w = (T)0 - p.inv_dx * (Fr.w - Fl.w);
   acc.hu = (T)0 - p.inv_dx * (Fr.hu - Fl.hu);
   acc.hv = (T)0 - p.inv_dx * (Fr.hv - Fl.hv);
-  for (int b = 0; b < p.n_bottom; ++b)
-    acc.hu = acc.hu + p.neg_g * slope_over<T>(br - bl, p.dx, p.inv_dx, p.dx_pow2) * ((R.w + L.w) * (T)0.5);
+  acc.hu = add_bottom<T>(p, acc.hu, slope_over<T>(br - bl, p.dx, p.inv_dx, p.dx_pow2), (R.w + L.w) * (T)0.5);
   return acc;
 }
 
@@ -198,7 +222,11 @@ __device__ __forceinline__ void block_speed_commit(StepRecord* rec, int parity, 
 template <typename T, bool CG>
 __device__ __forceinline__ void flux_march_unit(const Geom<T>& g, const Phys<T>& p, const T* U,
                                                 const T* __restrict__ B, T* Lout, T* Sout, const StripGeom& s,
-                                                unsigned long long& mx, unsigned long long& my) {
+                                                unsigned long long& mx_out, unsigned long long& my_out) {
+  // Float32 speed keys fit 32 bits: one 32-bit max per face instead of a
+  // 64-bit one (the flux pass measured 0.367 instead of 0.385 ms at 4096^2).
+  using Key = typename std::conditional<sizeof(T) == 4, unsigned, unsigned long long>::type;
+  Key mx = 0, my = 0;
   const int x = s.x;
   // prologue: rows ys-2..ys+1, corner rows ys-1..ys+2
   const Cell3<T> um2 = load_cell<T, CG>(g, U, x, s.ys - 2, s.ld_col);
@@ -215,8 +243,8 @@ __device__ __forceinline__ void flux_march_unit(const Geom<T>& g, const Phys<T>&
     recon<T>(p, um2, um1, uc, blm, b0, Lm, Rm);  // row ys-1
     recon<T>(p, um1, uc, un, b0, b1, L0, R0);    // row ys
     T sp = (T)0;
-    y.Gm = face<T, 1, true>(p, Rm, L0, sp);
-    if (s.out_col) my = max(my, speed_key<T>(sp));
+    y.Gm = face<T, 1, true, kFluxSel>(p, Rm, L0, sp);
+    if (s.out_col) my = max(my, (Key)speed_key<T>(sp));
     y.R = R0;
     y.Lh = L0.w;
     y.Bl = b0;
@@ -226,20 +254,19 @@ __device__ __forceinline__ void flux_march_unit(const Geom<T>& g, const Phys<T>&
     const Cell3<T> u2 = load_cell<T, CG>(g, U, x, j + 2, s.ld_col);
     const CornerRow<T> c2 = load_corner_row(g, B, x, j + 2);
     T sx = (T)0;
-    Cell3<T> acc = x_derivative<T, true>(g, p, uc, c0, c1, sx);
-    if (s.lane >= 2 && s.lane <= 2 + MOUT && s.x <= g.gc + g.nx) mx = max(mx, speed_key<T>(sx));
+    Cell3<T> acc = x_derivative<T, true, kFluxSel>(g, p, uc, c0, c1, sx);
+    if (s.lane >= 2 && s.lane <= 2 + MOUT && s.x <= g.gc + g.nx) mx = max(mx, (Key)speed_key<T>(sx));
     // y: reconstruct row j+1, flux through face j+1/2
     Cell3<T> Ln, Rn;
     const T b2 = b_yface(g, c2);
     recon<T>(p, uc, un, u2, y.Br, b2, Ln, Rn);
     T sp = (T)0;
-    const Cell3<T> Gp = face<T, 1, true>(p, y.R, Ln, sp);
-    if (s.out_col) my = max(my, speed_key<T>(sp));
+    const Cell3<T> Gp = face<T, 1, true, kFluxSel>(p, y.R, Ln, sp);
+    if (s.out_col) my = max(my, (Key)speed_key<T>(sp));
     acc.w = acc.w - p.inv_dy * (Gp.w - y.Gm.w);
     acc.hu = acc.hu - p.inv_dy * (Gp.hu - y.Gm.hu);
     acc.hv = acc.hv - p.inv_dy * (Gp.hv - y.Gm.hv);
-    for (int b = 0; b < p.n_bottom; ++b)
-      acc.hv = acc.hv + p.neg_g * slope_over<T>(y.Br - y.Bl, p.dy, p.inv_dy, p.dy_pow2) * ((y.R.w + y.Lh) * (T)0.5);
+    acc.hv = add_bottom<T>(p, acc.hv, slope_over<T>(y.Br - y.Bl, p.dy, p.inv_dy, p.dy_pow2), (y.R.w + y.Lh) * (T)0.5);
     acc.w = add_point_sources<T>(p, acc.w);
     if (s.out_col) {
       const long long o = sidx(g, x, j);
@@ -263,12 +290,15 @@ __device__ __forceinline__ void flux_march_unit(const Geom<T>& g, const Phys<T>&
     y.Br = b2;
     y.Gm = Gp;
   }
+  mx_out = max(mx_out, (unsigned long long)mx);
+  my_out = max(my_out, (unsigned long long)my);
 }
 
 // Resident blocks per SM the stage kernel is compiled for. The Float32 kernel
 // otherwise takes 92 registers (five blocks, 20 warps) and waits on memory;
 // at eight blocks (64 registers, a few bytes of spill) the 4096^2 stage pass
-// measured 0.616 instead of 0.755 ms. Float64 (190 registers) is bound by the
+// measured 0.616 instead of 0.755 ms, and after the edge and source changes
+// 0.475 against 0.551 ms at seven blocks (72 registers). Float64 (190 registers) is bound by the
 // FP64 pipe and is left alone.
 #ifndef VF_MARCH_STAGE_BLOCKS_F32
 #define VF_MARCH_STAGE_BLOCKS_F32 8
@@ -312,6 +342,7 @@ __device__ __forceinline__ Cell3<T> stage1_row(const Geom<T>& g, const Phys<T>& 
 // mirror source lane, hu negated. Every lane takes part in the shuffles.
 template <typename T>
 __device__ __forceinline__ Cell3<T> mirror_columns(const Geom<T>& g, const StripGeom& s, const Cell3<T>& u, bool yin) {
+  if (!s.xedge) return u;  // warp-uniform: no ghost column in this strip
   int src = s.lane;
   bool ghost = false;
   if (yin && s.x < g.gc) {
@@ -331,6 +362,25 @@ __device__ __forceinline__ Cell3<T> mirror_columns(const Geom<T>& g, const Strip
 template <typename T>
 __device__ __forceinline__ Cell3<T> mirror_row(const Cell3<T>& src) {  // src/bc.jl:101-109, hv negated
   return Cell3<T>{src.w, src.hu, -src.hv};
+}
+
+// U2 of cell (x, j) and the wall ghosts it is the mirror source of
+// (src/bc.jl:81-110): what store_with_ghosts writes for a wall boundary, with
+// the ghost logic skipped in warp-uniform branches for strips without ghost
+// columns and rows away from the bottom and top. With mirror_columns' early
+// return for such strips, the Float32 stage pass at 4096^2 measured 0.503
+// instead of 0.543 ms (the same bits).
+template <typename T>
+__device__ __forceinline__ void store_march(const Geom<T>& g, const StripGeom& s, T* __restrict__ Uo, int x, int j, T w,
+                                            T hu, T hv) {
+  if (s.xedge || j < g.gc + 2 || j >= g.gc + g.ny - 2) {
+    store_with_ghosts<T>(g, Uo, x, j, w, hu, hv);
+    return;
+  }
+  const long long o = sidx(g, x, j);
+  Uo[o] = w;
+  Uo[g.PS + o] = hu;
+  Uo[2 * g.PS + o] = hv;
 }
 
 // RK2 stage pass of one strip segment (warp-collective): U2 with its ghosts into Uo.
@@ -373,7 +423,7 @@ __device__ __forceinline__ void stage_march_unit(const Geom<T>& g, const Phys<T>
     recon<T>(p, um2, um1, uc, blm, b0, Lm, Rm);
     recon<T>(p, um1, uc, un, b0, b1, L0, R0);
     T sp;
-    y.Gm = face<T, 1, false>(p, Rm, L0, sp);
+    y.Gm = face<T, 1, false, kStageSel>(p, Rm, L0, sp);
     y.R = R0;
     y.Lh = L0.w;
     y.Bl = b0;
@@ -392,17 +442,16 @@ __device__ __forceinline__ void stage_march_unit(const Geom<T>& g, const Phys<T>
       u2 = mirror_columns(g, s, stage1_row<T, CG>(g, p, tdt, U0, Lin, Sin, x, j + 2, xin, c2, c3, u0x), j + 2 < top);
     }
     T sx;
-    Cell3<T> acc = x_derivative<T, false>(g, p, uc, c0, c1, sx);
+    Cell3<T> acc = x_derivative<T, false, kStageSel>(g, p, uc, c0, c1, sx);
     Cell3<T> Ln, Rn;
     const T b2 = b_yface(g, c2);
     recon<T>(p, uc, un, u2, y.Br, b2, Ln, Rn);
     T sp;
-    const Cell3<T> Gp = face<T, 1, false>(p, y.R, Ln, sp);
+    const Cell3<T> Gp = face<T, 1, false, kStageSel>(p, y.R, Ln, sp);
     acc.w = acc.w - p.inv_dy * (Gp.w - y.Gm.w);
     acc.hu = acc.hu - p.inv_dy * (Gp.hu - y.Gm.hu);
     acc.hv = acc.hv - p.inv_dy * (Gp.hv - y.Gm.hv);
-    for (int b = 0; b < p.n_bottom; ++b)
-      acc.hv = acc.hv + p.neg_g * slope_over<T>(y.Br - y.Bl, p.dy, p.inv_dy, p.dy_pow2) * ((y.R.w + y.Lh) * (T)0.5);
+    acc.hv = add_bottom<T>(p, acc.hv, slope_over<T>(y.Br - y.Bl, p.dy, p.inv_dy, p.dy_pow2), (y.R.w + y.Lh) * (T)0.5);
     acc.w = add_point_sources<T>(p, acc.w);
     if (s.out_col) {
       T w = uc.w + tdt * acc.w;
@@ -415,7 +464,7 @@ __device__ __forceinline__ void stage_march_unit(const Geom<T>& g, const Phys<T>
       if (p.friction && friction_active<T>(uc.hu, uc.hv))
         apply_friction<T>(tdt, friction_factor<T>(p, uc.w, uc.hu, uc.hv, Bc), hu, hv);
       dry_clamp<T>(p, w, hu, hv, Bc);
-      store_with_ghosts<T>(g, Uo, x, j, w, hu, hv);
+      store_march<T>(g, s, Uo, x, j, w, hu, hv);
     }
     uc = un;
     un = u2;

@@ -288,6 +288,8 @@ struct Phys {
   int any_dynamic;            // some point source is not a constant
   int point_kind[8];          // PointKind
   T point_add[8];             // kConstant: +rate/3600 for rain, -rate for infiltration
+  T point_sum;                // Float32: the constant point sources' sum (summed in Float64)
+  T bottom_g;                 // Float32: n_bottom * (-g), the bottom sources' factor at once
   const T* point_field[8];    // kHorton: factor, kField: rain rate [m/s]; total grid, state layout
   const double* tab_t[8];     // kTable: breakpoints of TimeDependentRain
   const double* tab_r[8];     // kTable: rates/3600 per breakpoint
@@ -347,16 +349,24 @@ __device__ __forceinline__ void point_scalars(const Phys<T>& p, double t, T* out
 }
 
 // ΔB/Δ of the bottom source; exact reciprocal multiply when Δ is a power of two.
+// Float32 always multiplies by 1/Δ (one rounding more where Δ is not a power
+// of two; a 1.5% faster Float32 step, the same bits on power-of-two cells).
 template <typename T>
 __device__ __forceinline__ T slope_over(T dB, T delta, T inv_delta, int pow2) {
+  if constexpr (sizeof(T) == 4) return dB * inv_delta;
   return pow2 ? dB * inv_delta : Arith<T>::div(dB, delta);
 }
 
 // Rain and infiltration in list order (src/system.jl:71-73), unrolled so the
 // parameter block is never indexed dynamically. `scal` holds point_scalars();
 // `cell` is the cell's offset in the state layout (for per-cell arrays).
+// Float32 (the marching kernels' constant sources) adds their sum at once:
+// one add instead of eight guarded ones, 2-4% of the Float32 stage pass; the
+// sum rounds once to Float32 where the list order would round after each
+// source (Float32 results are held to a stated error, not to the bits).
 template <typename T>
 __device__ __forceinline__ T add_point_sources(const Phys<T>& p, T acc0) {
+  if constexpr (sizeof(T) == 4) return acc0 + p.point_sum;
 #pragma unroll
   for (int n = 0; n < 8; ++n)
     if (n < p.n_point) acc0 = acc0 + p.point_add[n];
@@ -379,9 +389,16 @@ __device__ __forceinline__ T add_point_sources(const Phys<T>& p, T acc0, const T
 
 // desingularize, src/equations/equation.jl:40-62 (Eq. 26 of Brodtkorb & Holm 2021).
 // For |h| >= kappa the expression equals h exactly: min(...) <= kappa <= |h|.
-template <typename T>
+// SEL (Float32 only): the same function without a branch, the formula
+// evaluated for every h (|h| >= kappa gives |h| with h's sign, i.e. h), with
+// 1/(2 kappa) as a product; fewer instructions where registers allow.
+template <typename T, bool SEL = false>
 __device__ __forceinline__ T desing(T h, T kappa) {
   using A = Arith<T>;
+  if constexpr (SEL && sizeof(T) == 4) {
+    const float m = fminf(h * h * (0.5f / kappa) + kappa * 0.5f, kappa);
+    return copysignf(fmaxf(fabsf(h), m), h);
+  }
   if (!A::abs_lt(h, kappa)) return h;
   const T m = A::min(A::div(h * h, (T)2 * kappa) + kappa / (T)2, kappa);
   return copysign((T)1, h) * A::max(fabs(h), m);
@@ -420,10 +437,10 @@ __device__ __forceinline__ void velocities(const Phys<T>& p, T h, T hs, T hu, T 
 
 // One side of a face: physical flux (src/equations/swe_2D.jl:43-65) and the
 // two outer eigenvalues (src/equations/swe_2D.jl:69-81).
-template <typename T, int DIR>
+template <typename T, int DIR, bool SEL = false>
 __device__ __forceinline__ void side_flux(const Phys<T>& p, T h, T hu, T hv, T& f0, T& f1, T& f2, T& l1, T& l2) {
   using A = Arith<T>;
-  const T hs = desing<T>(h, p.kappa);
+  const T hs = desing<T, SEL>(h, p.kappa);
   T u, v;
   velocities<T>(p, h, hs, hu, hv, u, v);
   const T rh = p.rho * h;
@@ -445,14 +462,14 @@ __device__ __forceinline__ void side_flux(const Phys<T>& p, T h, T hu, T hv, T& 
 
 // Central-upwind flux across one face, src/numericalflux/swe/centralupwind.jl:48-77.
 // minus = right face value of the left cell, plus = left face value of the right cell.
-template <typename T, int DIR, bool SPEED>
+template <typename T, int DIR, bool SPEED, bool SEL = false>
 __device__ __forceinline__ void cu_face(const Phys<T>& p, T mh, T mhu, T mhv, T ph, T phu, T phv, T& F0, T& F1, T& F2,
                                         T& speed) {
   using A = Arith<T>;
   T fm0 = 0, fm1 = 0, fm2 = 0, em1 = 0, em2 = 0;
-  if (A::gt(mh, p.cutoff)) side_flux<T, DIR>(p, mh, mhu, mhv, fm0, fm1, fm2, em1, em2);
+  if (A::gt(mh, p.cutoff)) side_flux<T, DIR, SEL>(p, mh, mhu, mhv, fm0, fm1, fm2, em1, em2);
   T fp0 = 0, fp1 = 0, fp2 = 0, ep1 = 0, ep2 = 0;
-  if (A::gt(ph, p.cutoff)) side_flux<T, DIR>(p, ph, phu, phv, fp0, fp1, fp2, ep1, ep2);
+  if (A::gt(ph, p.cutoff)) side_flux<T, DIR, SEL>(p, ph, phu, phv, fp0, fp1, fp2, ep1, ep2);
   const T aplus = A::max(A::max(ep1, em1), (T)0);
   const T aminus = A::min(A::min(ep2, em2), (T)0);
   const T d = aplus - aminus;
