@@ -366,11 +366,14 @@ __device__ __forceinline__ T slope_over(T dB, T delta, T inv_delta, int pow2) {
 // source (Float32 results are held to a stated error, not to the bits).
 template <typename T>
 __device__ __forceinline__ T add_point_sources(const Phys<T>& p, T acc0) {
-  if constexpr (sizeof(T) == 4) return acc0 + p.point_sum;
+  if constexpr (sizeof(T) == 4) {
+    return acc0 + p.point_sum;
+  } else {
 #pragma unroll
-  for (int n = 0; n < 8; ++n)
-    if (n < p.n_point) acc0 = acc0 + p.point_add[n];
-  return acc0;
+    for (int n = 0; n < 8; ++n)
+      if (n < p.n_point) acc0 = acc0 + p.point_add[n];
+    return acc0;
+  }
 }
 template <typename T>
 __device__ __forceinline__ T add_point_sources(const Phys<T>& p, T acc0, const T* scal, long long cell) {
