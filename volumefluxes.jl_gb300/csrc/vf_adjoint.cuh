@@ -46,8 +46,11 @@ template <typename T>
 __device__ __forceinline__ Dual<T> operator-(Dual<T> a, Dual<T> b) { return Dual<T>(a.v - b.v, a.d - b.d); }
 template <typename T>
 __device__ __forceinline__ Dual<T> operator-(Dual<T> a) { return Dual<T>(-a.v, -a.d); }
+// Derivative parts use fused multiply-adds and reciprocals where the value
+// parts keep the forward pass's exact operations: values and branches stay
+// the forward pass's, derivatives change at the rounding level only.
 template <typename T>
-__device__ __forceinline__ Dual<T> operator*(Dual<T> a, Dual<T> b) { return Dual<T>(a.v * b.v, a.d * b.v + a.v * b.d); }
+__device__ __forceinline__ Dual<T> operator*(Dual<T> a, Dual<T> b) { return Dual<T>(a.v * b.v, fma(a.d, b.v, a.v * b.d)); }
 template <typename T>
 __device__ __forceinline__ Dual<T> operator/(Dual<T> a, Dual<T> b) {
   const T q = a.v / b.v;
@@ -78,7 +81,7 @@ struct Arith<Dual<T>> {
   static __device__ __forceinline__ D min(D x, D y) { return picks_second_min(x.v, y.v) ? y : x; }
   static __device__ __forceinline__ D div(D a, D b) {
     const T q = A::div(a.v, b.v);
-    return D(q, (a.d - q * b.d) / b.v);
+    return D(q, fma(-q, b.d, a.d) * A::inv(A::recip(b.v)));
   }
   static __device__ __forceinline__ D rcp(D b) {
     const T r = A::rcp(b.v);
@@ -86,7 +89,7 @@ struct Arith<Dual<T>> {
   }
   static __device__ __forceinline__ D sqrt_(D x) {
     const T r = A::sqrt_(x.v);
-    return D(r, r > (T)0 ? x.d / ((T)2 * r) : (T)0);
+    return D(r, r > (T)0 ? x.d * ((T)0.5 * A::inv(A::recip(r))) : (T)0);
   }
   // Quotients over one divisor: values as the forward's div_by, derivatives of a/b.
   struct Recip {
@@ -96,7 +99,7 @@ struct Arith<Dual<T>> {
   static __device__ __forceinline__ Recip recip(D b) { return Recip{b, A::recip(b.v)}; }
   static __device__ __forceinline__ D div_by(const Recip& R, D a) {
     const T q = A::div_by(R.R, a.v);
-    return D(q, (a.d - q * R.b.d) / R.b.v);
+    return D(q, fma(-q, R.b.d, a.d) * A::inv(R.R));
   }
   // For equal values the forward max/min may return either operand; these
   // say which, so the derivative follows the same operand.
@@ -113,7 +116,7 @@ struct Arith<Dual<T>> {
 template <>
 __device__ __forceinline__ Dual<double> vcbrt<Dual<double>>(Dual<double> x) {
   const double r = vcbrt<double>(x.v);
-  return Dual<double>(r, x.v != 0.0 ? x.d * r / (3.0 * x.v) : 0.0);
+  return Dual<double>(r, x.v != 0.0 ? x.d * r * Arith<double>::inv(Arith<double>::recip(3.0 * x.v)) : 0.0);
 }
 template <>
 __device__ __forceinline__ Dual<float> vcbrt<Dual<float>>(Dual<float> x) {

@@ -103,6 +103,7 @@ struct Arith<double> {
   };
   static __device__ __forceinline__ Recip recip(double b) { return Recip{rcp(b)}; }
   static __device__ __forceinline__ double div_by(const Recip& R, double a) { return a * R.r; }
+  static __device__ __forceinline__ double inv(const Recip& R) { return R.r; }
 #elif VF_FP64_MARKSTEIN
   // Correctly rounded quotients through a correctly rounded reciprocal
   // (Markstein, IBM J. Res. Dev. 34(1), 1990; Cornea, Harrison & Tang,
@@ -145,6 +146,9 @@ struct Arith<double> {
   }
   static __device__ __forceinline__ double div(double a, double b) { return div_by(recip(b), a); }
   static __device__ __forceinline__ double rcp(double b) { return div(1.0, b); }
+  // 1/b for terms that need no correct rounding (the derivative parts of
+  // dual numbers): the correctly rounded reciprocal, where the method applies.
+  static __device__ __forceinline__ double inv(const Recip& R) { return R.ok ? R.y : 1.0 / R.b; }
   static __device__ __forceinline__ double sqrt_(double x) { return sqrt(x); }
 #else
   // Correctly rounded division and square root on the FP64 pipe, one IEEE
@@ -160,6 +164,7 @@ struct Arith<double> {
   };
   static __device__ __forceinline__ Recip recip(double b) { return Recip{b}; }
   static __device__ __forceinline__ double div_by(const Recip& R, double a) { return a / R.b; }
+  static __device__ __forceinline__ double inv(const Recip& R) { return 1.0 / R.b; }
 #endif  // VF_FP64_FAITHFUL
 };
 
@@ -183,6 +188,7 @@ struct Arith<float> {
   };
   static __device__ __forceinline__ Recip recip(float b) { return Recip{rcp(b)}; }
   static __device__ __forceinline__ float div_by(const Recip& R, float a) { return a * R.r; }
+  static __device__ __forceinline__ float inv(const Recip& R) { return R.r; }
 };
 
 // ---------------------------------------------------------------------------
