@@ -298,13 +298,15 @@ __device__ __forceinline__ void flux_march_unit(const Geom<T>& g, const Phys<T>&
 // otherwise takes 92 registers (five blocks, 20 warps) and waits on memory;
 // at eight blocks (64 registers, a few bytes of spill) the 4096^2 stage pass
 // measured 0.616 instead of 0.755 ms, and after the edge and source changes
-// 0.475 against 0.551 ms at seven blocks (72 registers). Float64 (190 registers) is bound by the
-// FP64 pipe and is left alone.
+// 0.475 against 0.551 ms at seven blocks (72 registers). The Float32 flux
+// pass is held to seven blocks (72 registers, no spill): 0.319 instead of
+// 0.323 ms at its natural 77 registers and six blocks. Float64 (190
+// registers) is bound by the FP64 pipe and is left alone.
 #ifndef VF_MARCH_STAGE_BLOCKS_F32
 #define VF_MARCH_STAGE_BLOCKS_F32 8
 #endif
 #ifndef VF_MARCH_FLUX_BLOCKS_F32
-#define VF_MARCH_FLUX_BLOCKS_F32 1
+#define VF_MARCH_FLUX_BLOCKS_F32 7
 #endif
 template <typename T> struct MarchStageBlocks { static constexpr int value = sizeof(T) == 4 ? VF_MARCH_STAGE_BLOCKS_F32 : 1; };
 template <typename T> struct MarchFluxBlocks { static constexpr int value = sizeof(T) == 4 ? VF_MARCH_FLUX_BLOCKS_F32 : 1; };
