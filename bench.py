@@ -110,8 +110,8 @@ def kernel_names(dtype: str) -> dict:
     marching for Float32; VF_KERNELS and VF_TMA=0 override)."""
     variant = os.environ.get("VF_KERNELS", "tile" if dtype == "f64" else "march")
     t = "double" if dtype == "f64" else "float"
-    if variant == "march":
-        return {"flux": f"k_flux_march<{t},64>", "stage": f"k_stage_march<{t},64>"}
+    if variant == "march":  # template arguments: rows per segment of each pass
+        return {"flux": f"k_flux_march<{t},40>", "stage": f"k_stage_march<{t},24>"}
     if dtype == "f64" and os.environ.get("VF_TMA", "1") != "0":
         return {"flux": "k_flux_tma<double>", "stage": "k_stage2_tma<double>"}
     return {"flux": f"k_flux<{t}>", "stage": f"k_stage2<{t}>"}

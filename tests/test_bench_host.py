@@ -67,11 +67,11 @@ def test_kernel_names_follow_the_switches(monkeypatch):
     monkeypatch.delenv("VF_KERNELS", raising=False)
     monkeypatch.delenv("VF_TMA", raising=False)
     assert bench.kernel_names("f64") == {"flux": "k_flux_tma<double>", "stage": "k_stage2_tma<double>"}
-    assert bench.kernel_names("f32")["stage"] == "k_stage_march<float,64>"
+    assert bench.kernel_names("f32")["stage"] == "k_stage_march<float,24>"
     monkeypatch.setenv("VF_TMA", "0")
     assert bench.kernel_names("f64")["stage"] == "k_stage2<double>"
     monkeypatch.setenv("VF_KERNELS", "march")
-    assert bench.kernel_names("f64")["flux"] == "k_flux_march<double,64>"
+    assert bench.kernel_names("f64")["flux"] == "k_flux_march<double,40>"
 
 
 def test_cpu_baseline_timer_small_grid():
