@@ -300,3 +300,38 @@ def test_time_order_of_the_steppers():
     order = time_order(_oracle_run)
     assert order["rk2"] == pytest.approx(2.0, abs=0.05)
     assert order["fe"] == pytest.approx(1.0, abs=0.1)
+
+
+def _friction_run(nx, ny, B=None, bottom_constant=0.0, elevate=0.0, bottom_source=False, T=0.05):
+    """test/test_friction_1d.jl:25-43 in 2D: a Gaussian ridge along x,
+    LinearReconstruction(1.05), CentralUpwind, RK2, the default
+    ImplicitFriction (Cz = 0.03^2, friction_bh2021), CFL 0.2, to T = 0.05."""
+    x = (np.arange(nx) + 0.5) / nx
+    w0 = (np.exp(-(x - 0.5) ** 2 / 0.001) + 1.5 + elevate)[:, None] * np.ones((nx, ny))
+    z = np.zeros_like(w0)
+    o = O.OracleSim(nx=nx, ny=ny, cfl=0.2, stepper=O.STEPPER_RK2, theta=1.05, friction=O.FRICTION_BH2021,
+                    friction_Cz=0.03 ** 2, B=B, bottom_constant=bottom_constant,
+                    sources=[(O.SRC_BOTTOM, 0.0)] if bottom_source else [])
+    o.set_interior(w0, z, z.copy())
+    o.simulate_to_time(T)
+    return o.interior()
+
+
+def test_friction_run_is_invariant_under_a_raised_bottom():
+    # test/test_friction_1d.jl:83-115: the same run with the bottom and the
+    # initial surface raised by 1 (a constant bottom and a bottom field of
+    # ones, both with SourceTermBottom) gives the flat-bottom depths and
+    # momenta; the reference allows 1e-2 summed over the cells, the oracle
+    # holds 1e-10 (what remains is the rounding of w + 1).
+    nx, ny = 256, 4
+    h_ref, hu_ref, _ = _friction_run(nx, ny)
+    const = _friction_run(nx, ny, bottom_constant=1.0, elevate=1.0, bottom_source=True)
+    field = _friction_run(nx, ny, B=np.ones((nx + 5, ny + 5)), elevate=1.0, bottom_source=True)
+    for h, hu, hv in (const, field):
+        assert np.sum(np.abs(h_ref - (h - 1.0))) <= 1e-10
+        assert np.sum(np.abs(hu_ref - hu)) <= 1e-10
+        assert np.all(hv == 0.0)
+    # a bottom field of ones gives B_cell = ((1 + 1) + 1) + 1) / 4 = 1 exactly:
+    # the constant and the field run are the same bits
+    for a, b in zip(const, field):
+        assert np.array_equal(a, b)
