@@ -109,3 +109,29 @@ def test_scenarios_shapes():
     assert sc.B.shape == (69, 69) and sc.w0.shape == (64, 64)
     Bc = 0.25 * (sc.B[:-1, :-1] + sc.B[1:, :-1] + sc.B[:-1, 1:] + sc.B[1:, 1:])[2:-2, 2:-2]
     assert np.all(sc.w0 >= Bc) and np.any(sc.w0 == Bc)  # dry islands exist
+
+
+def test_grid_coordinates_2d():
+    # test/test_grid_2d.jl:25-85: a 10 x 6 grid over [0,10] x [0,6] with gc = 2
+    nx, ny, gc = 10, 6, 2
+    g = vf.CartesianGrid(nx, ny, extent=[[0.0, nx], [0.0, ny]], gc=gc)
+    dx, dy = vf.compute_dx(g), vf.compute_dy(g)
+    faces, centers = vf.cell_faces(g), vf.cell_centers(g)
+    assert np.array_equal(faces[:, :, 0], np.arange(nx + 1.0)[:, None] * np.ones((1, ny + 1)))
+    assert np.array_equal(faces[:, :, 1], np.ones((nx + 1, 1)) * np.arange(ny + 1.0)[None, :])
+    assert np.array_equal(centers[:, :, 0], (np.arange(nx) + 0.5)[:, None] * np.ones((1, ny)))
+    assert np.array_equal(centers[:, :, 1], np.ones((nx, 1)) * (np.arange(ny) + 0.5)[None, :])
+    assert np.array_equal(vf.cell_faces(g, vf.XDIR), np.arange(nx + 1.0))
+    assert np.array_equal(vf.cell_faces(g, vf.YDIR), np.arange(ny + 1.0))
+    assert np.array_equal(vf.cell_centers(g, vf.XDIR), np.arange(nx) + 0.5)
+    assert np.array_equal(vf.cell_centers(g, vf.YDIR), np.arange(ny) + 0.5)
+    faces_gc = vf.cell_faces(g, interior=False)
+    assert np.allclose(faces_gc[2:-2, 2:-2], faces, rtol=0, atol=1e-14)
+    cells_gc = vf.cell_centers(g, interior=False)
+    assert np.allclose(cells_gc[2:-2, 2:-2], centers, rtol=0, atol=1e-14)
+    for j in (1, 2):
+        for i in (1, 2):
+            assert np.allclose(faces_gc[i - 1, j - 1], (-3 + i, -3 + j), rtol=0, atol=1e-14)
+            assert np.allclose(faces_gc[-i, -j], (nx + (gc - i + 1), ny + (gc - j + 1)), rtol=0, atol=1e-14)
+            assert np.allclose(cells_gc[i - 1, j - 1], (-3 + i + dx / 2, -3 + j + dy / 2), rtol=0, atol=1e-14)
+            assert np.allclose(cells_gc[-i, -j], (nx + (gc - i) + dx / 2, ny + (gc - j) + dy / 2), rtol=0, atol=1e-14)

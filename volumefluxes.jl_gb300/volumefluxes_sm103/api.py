@@ -126,8 +126,13 @@ def cell_faces(grid: CartesianGrid, direction: int | None = None, interior: bool
     return out
 
 
-def cell_centers(grid: CartesianGrid, interior: bool = True) -> np.ndarray:
-    """Cell centres, src/grid.jl:151-161: face intersection + (dx, dy)/2. Shape (nx, ny, 2)."""
+def cell_centers(grid: CartesianGrid, direction: int | None = None, interior: bool = True) -> np.ndarray:
+    """Cell centres, src/grid.jl:151-161: face intersection + (dx, dy)/2, shape
+    (nx, ny, 2). With a direction (src/grid.jl:145-149): the 1D centres along
+    it, faces[:-1] + (faces[1] - faces[0])/2."""
+    if direction is not None:
+        f1 = cell_faces(grid, direction, interior=interior)
+        return f1[:-1] + (f1[1] - f1[0]) / 2.0
     f = cell_faces(grid, interior=interior)
     c = f[:-1, :-1, :].copy()
     c[:, :, 0] += compute_dx(grid) / 2
